@@ -1,0 +1,286 @@
+#!/usr/bin/env python
+"""Decoded info Gbit/s of the BICM-LDPC Monte Carlo trial on GB300, and its CPU baseline.
+
+Workload (one "step" = one launch batch): 5G NR LDPC base graph 1, Z = 384, K' = 8448,
+E = 25344 (rate 1/3), Gray 16-QAM, AWGN at Eb/N0 in 0:0.25:2 dB, max-log LLRs, layered
+normalised min-sum alpha = 0.75, at most 20 iterations with the syndrome stop, f32 LLRs
+and messages, 8192 codewords per launch.  Step s runs grid point s mod 9 on the next
+8192 frames of that condition; frame f of condition c is drawn from
+stream(seed = 7, "bicm_ldpc_c2", c, f).  The stop rule of the campaign (500 frame errors
+or 1e6 frames per point) ends every point of this grid after its first batch (FER ~ 1),
+so 9 steps are the whole campaign.
+
+--impl ours (default): `value` = device-timed throughput of the frame generator and
+the decoder (inputs: the frames' streams; every launch writes 830 MB of LLRs, more than
+L2); `e2e` = the same through the public C ABI call cb_run_frames with the per-frame
+records returned to pinned host memory every step; `roofline` = the decoder kernel
+against the measured HBM copy bandwidth.
+--impl reference: the CPU oracle's restatement of the reference trial (f64, the
+reference's libm noise) on all host cores, a bounded sample of frames per step.
+"""
+
+import argparse
+import ctypes as C
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "decoded info Gbit/s at equal FER, neural vs plain min-sum; vs CPU Runner"
+K_INFO, E, BG, Z, M = 8448, 25344, 1, 384, 16
+GRID = [0.25 * i for i in range(9)]
+SEED, NAME = 7, "bicm_ldpc_c2"
+# algorithmic bytes of one decoded codeword: E f32 LLRs in, ceil(K'/8) decision bytes out,
+# a 4-byte record (iteration count)
+ALGO_BYTES = E * 4 + (K_INFO + 7) // 8 + 4
+WORKLOAD = ("5G NR LDPC BG1 Z=384 K'=8448 E=25344 (rate 1/3), Gray 16-QAM, AWGN Eb/N0 0:0.25:2 dB, "
+            "max-log LLRs, layered NMS alpha=0.75, <=20 iterations + syndrome stop, f32, 8192 codewords/launch")
+
+
+def read_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.rows, self.proc = device, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_sample(steps, warmup, threads=0, budget_s=2.0):
+    """The oracle's trial (f64, libm noise, as the reference) over all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    cores = threads or os.cpu_count()
+    code = O.Code(K_INFO, E, bg=BG, z=Z).set_decoder(O.RULE_NMS, 0.75, True, 20)
+    h = O.fnv1a64(NAME)
+    # size the per-step sample from a first timing: about budget_s of work per step
+    t0 = time.perf_counter()
+    code.run_frames(M, SEED, h, 0, 0, cores, GRID[0], 0, O.NOISE_LIBM, cores)
+    per = (time.perf_counter() - t0) / cores
+    n = max(cores, int(budget_s / per / cores) * cores)
+    for s in range(warmup):
+        code.run_frames(M, SEED, h, s % 9, 10_000_000 + s * n, n, GRID[s % 9], 0, O.NOISE_LIBM, cores)
+    total_t, frames, fe = 0.0, 0, 0
+    for s in range(steps):
+        t0 = time.perf_counter()
+        r = code.run_frames(M, SEED, h, s % 9, (s // 9) * n, n, GRID[s % 9], 0, O.NOISE_LIBM, cores)
+        total_t += time.perf_counter() - t0
+        frames += n
+        fe += int(r["frame_error"].sum())
+    gbps = frames * K_INFO / total_t / 1e9
+    return gbps, cores, n, frames, total_t, fe / frames
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    gbps, cores, n, frames, t, fer = cpu_sample(args.steps, args.warmup)
+    sample = (f"{n} frames per step ({frames} in {args.steps} steps, {t:.1f} s) of the same workload, "
+              f"one frame per Runner trial, f64 decoder and libm noise as the reference")
+    line = {"impl": "reference", "metric": METRIC, "value": gbps, "unit": "Gbit/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "frames_per_step": n, "fer": fer},
+            "cpu_baseline": {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": gbps, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    cb = importlib.import_module("com-rs_gb300")
+    L = cb.lib()
+    B = args.frames
+    code = cb.NrLdpc(K_INFO, E, base_graph=BG, lifting_size=Z, precision="f32", device=local_rank)
+    h = code._h
+    nh = cb.fnv1a64(NAME)
+    results = torch.empty(B * 8, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def step(s):
+        cond = s % 9
+        first = (s // 9) * B * world + rank * B
+        st = L.cb_run_frames_device(h, M, SEED, nh, cond, first, B, GRID[cond], C.c_void_p(results.data_ptr()), sp)
+        if st:
+            raise cb.ComrsError(st, L.cb_last_error(h).decode())
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for s in range(args.warmup):
+        step(10_000 + s)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fer_acc, it_acc = [], []
+    with ClockSampler(local_rank) as clocks:
+        ev0.record(stream)
+        for s in range(args.steps):
+            step(s)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = max_over_ranks(ev0.elapsed_time(ev1))
+    rec = results.cpu().numpy().view(cb.FRAME_DTYPE)
+    fer_acc.append(float(rec["frame_error"].mean()))
+    it_acc.append(float(rec["iterations"].mean()))
+    value = args.steps * B * world * K_INFO / (ms * 1e-3) / 1e9
+
+    # roofline of the decoder kernel: LLRs already in HBM, CUDA events around its launch
+    llr = torch.empty((B, E), dtype=torch.float32, device="cuda")
+    info = torch.empty((B, (K_INFO + 31) // 32), dtype=torch.int32, device="cuda")
+    bits = torch.empty((B, (K_INFO + 31) // 32), dtype=torch.int32, device="cuda")
+    iters = torch.empty(B, dtype=torch.int32, device="cuda")
+    dec_ms, gen_ms = [], []
+    for rep in range(4):
+        cond = rep % 9
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        st = L.cb_generate_frames_device(h, M, SEED, nh, cond, 1_000_000 + rep * B, B, GRID[cond],
+                                         C.c_void_p(llr.data_ptr()), C.c_void_p(info.data_ptr()), sp)
+        e1.record(stream)
+        st |= L.cb_decode_device(h, C.c_void_p(llr.data_ptr()), B, C.c_void_p(bits.data_ptr()), None,
+                                 C.c_void_p(iters.data_ptr()), sp)
+        e2.record(stream)
+        torch.cuda.synchronize()
+        if st:
+            raise cb.ComrsError(st, L.cb_last_error(h).decode())
+        if rep:  # the first repetition is a warm-up
+            gen_ms.append(e0.elapsed_time(e1))
+            dec_ms.append(e1.elapsed_time(e2))
+    dec = float(np.mean(dec_ms))
+    achieved = B * ALGO_BYTES / (dec * 1e-3) / 1e9
+    peaks = read_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "layered_kernel<float,19> (decoder)",
+                "algorithmic_bytes_per_launch": B * ALGO_BYTES, "launch_ms": dec,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+                "generator_launch_ms": float(np.mean(gen_ms))}
+
+    # end to end through the public C ABI: per-frame records to pinned host memory
+    host = torch.empty(B * 8, dtype=torch.uint8, pin_memory=True)
+    out_p = C.c_void_p(host.data_ptr())
+    for s in range(2):
+        L.cb_run_frames(h, M, SEED, nh, s % 9, 2_000_000 + s * B, B, GRID[s % 9], out_p)
+    barrier()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        cond = s % 9
+        first = (s // 9) * B * world + rank * B
+        st = L.cb_run_frames(h, M, SEED, nh, cond, first, B, GRID[cond], out_p)
+        if st:
+            raise cb.ComrsError(st, L.cb_last_error(h).decode())
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = {"value": args.steps * B * world * K_INFO / e2e_s / 1e9, "unit": "Gbit/s", "h2d_bytes_per_step": 0,
+           "d2h_bytes_per_step": B * 8, "api": "cb_run_frames (host records)",
+           "inputs": "the frames' streams (seed, name, condition, frame index) passed as arguments"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        gbps, cores, n, frames, t, _ = cpu_sample(2, 0, budget_s=5.0)
+        cpu = {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port",
+               "sample": f"{frames} frames ({t:.1f} s) of the same workload, grid points 0 and 0.25 dB, f64 decoder "
+                         f"and libm noise as the reference"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (Monte Carlo frames from seeded streams)",
+                "config": {"workload": WORKLOAD, "codewords_per_launch": B, "ebn0_db": GRID,
+                           "l2": "inputs larger than L2: each step writes and reads 830 MB of LLRs",
+                           "parallelism": f"dp{world} (disjoint frame ranges per GPU)",
+                           "last_step_fer": fer_acc[-1], "last_step_mean_iterations": it_acc[-1]},
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
+                "gpu_launches": 2 * args.steps}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=9)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--frames", type=int, default=8192)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,240 @@
+"""comrs_gb300 -- the com-rs BICM-LDPC Monte Carlo trial on one GB300.
+
+Python front of ``libcomrs_gb300.so`` (C ABI: ``include/comrs_gb300.h``).  It mirrors
+the reference's Python surface for this path:
+
+* :class:`NrLdpc` -- ``comrs.NrLdpc(k, e, base_graph=, rv=, qm=, rule=, alpha=,
+  max_iterations=, layered=)`` (bindings/com-py/src/fec/nr.rs:52-83) with ``encode`` /
+  ``decode`` / ``app``, plus the explicit ``lifting_size`` and the GPU ``precision``;
+* :meth:`NrLdpc.run_frames` -- the Monte Carlo frames of one condition, frame f drawn
+  from ``stream(seed, name, condition, f)`` (crates/com-sim/src/runner.rs:435-447);
+* :func:`run` -- a campaign over an Eb/N0 grid with the ``min_errors(...).or(max_trials)``
+  stopping rule of com-sim (crates/com-sim/src/stopping.rs:64-265).
+
+The compute runs only in the CUDA library: there is no CPU fallback.  Importing works
+without a GPU; creating a code object needs one.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .campaign import Grid, Stop, run  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcomrs_gb300.so")
+
+RULES = {"normalized_min_sum": 1, "min_sum": 1, "offset_min_sum": 2, "sum_product": 0}
+PRECISIONS = {"f64": 0, "f32": 1}
+FRAME_DTYPE = np.dtype([("bit_errors", "<u4"), ("frame_error", "u1"), ("iterations", "u1"), ("reserved", "<u2")])
+
+
+class ComrsError(RuntimeError):
+    """A non-zero status of the C ABI (``cb_status``), with the library's message."""
+
+    KINDS = {-1: "Config", -2: "Shape", -3: "Numerical", -4: "Condition", -5: "Io", -6: "Cuda", -7: "Timeout"}
+
+    def __init__(self, status, message):
+        self.status = status
+        self.kind = self.KINDS.get(status, "Unknown")
+        super().__init__(f"{self.kind}: {message}")
+
+
+class _Desc(C.Structure):
+    _fields_ = [("k_info", C.c_int32), ("e", C.c_int32), ("base_graph", C.c_int32), ("lifting_size", C.c_int32),
+                ("rv", C.c_int32), ("qm", C.c_int32), ("rule", C.c_int32), ("alpha", C.c_double),
+                ("layered", C.c_int32), ("max_iterations", C.c_int32), ("precision", C.c_int32),
+                ("device", C.c_int32)]
+
+
+# (name, restype, argtypes) of every symbol of include/comrs_gb300.h
+_vp, _i32, _i64, _u64, _dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_double
+SYMBOLS = [
+    ("cb_version", C.c_char_p, []),
+    ("cb_code_create", _i32, [C.POINTER(_Desc), C.POINTER(_vp)]),
+    ("cb_code_destroy", None, [_vp]),
+    ("cb_last_error", C.c_char_p, [_vp]),
+    ("cb_code_info", _i32, [_vp, _vp]),
+    ("cb_code_tables", _i32, [_vp, _vp, _vp]),
+    ("cb_encode", _i32, [_vp, _vp, _i64, _vp]),
+    ("cb_decode", _i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    ("cb_decode_device", _i32, [_vp, _vp, _i64, _vp, _vp, _vp, _vp]),
+    ("cb_run_frames", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp]),
+    ("cb_generate_frames", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp]),
+    ("cb_run_frames_device", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp]),
+    ("cb_generate_frames_device", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp, _vp]),
+    ("cb_xoshiro_jump", _i32, [_vp, _u64, _vp]),
+]
+
+_lib = None
+
+
+def lib():
+    """The loaded CUDA library (raises if it was not built: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with __graft_entry__.build() or "
+                              "python com-rs_gb300/build.py (no CPU fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SYMBOLS:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _check(status, handle=None):
+    if status != 0:
+        msg = lib().cb_last_error(handle)
+        raise ComrsError(status, msg.decode() if msg else "")
+
+
+def fnv1a64(name):
+    """FNV-1a 64 of a scenario name (crates/com-core/src/rng.rs:58-65)."""
+    h = 0xCBF29CE484222325
+    for b in name.encode() if isinstance(name, str) else bytes(name):
+        h ^= b
+        h = (h * 0x100000001B3) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def version():
+    return lib().cb_version().decode()
+
+
+def xoshiro_jump(state, steps):
+    """The xoshiro256** state after `steps` draws (Rng::state / Rng::from_state)."""
+    s = np.ascontiguousarray(state, np.uint64)
+    out = np.zeros(4, np.uint64)
+    _check(lib().cb_xoshiro_jump(_p(s), steps, _p(out)))
+    return out
+
+
+class NrLdpc:
+    """The 5G NR LDPC code of K' information bits rate-matched to E bits, on a GPU.
+
+    Mirrors ``comrs.NrLdpc`` (bindings/com-py/src/fec/nr.rs:52-83); decoder defaults are
+    those of the benchmark configurations (layered normalised min-sum, alpha 0.75, 20
+    iterations).  ``precision`` is the arithmetic of LLRs and messages: ``"f64"`` (the
+    reference's, bit-exact) or ``"f32"``.
+    """
+
+    def __init__(self, k, e, base_graph=None, rv=0, qm=1, rule="normalized_min_sum", alpha=0.75,
+                 max_iterations=20, layered=True, lifting_size=None, precision="f64", device=0):
+        rule_l = rule.lower()
+        if rule_l not in RULES:
+            raise ComrsError(-1, f"rule must be one of {sorted(RULES)}, got {rule!r}")
+        if precision not in PRECISIONS:
+            raise ComrsError(-1, f"precision must be 'f64' or 'f32', got {precision!r}")
+        d = _Desc(k, e, base_graph or 0, lifting_size or 0, rv, qm, RULES[rule_l],
+                  1.0 if rule_l == "min_sum" else float(alpha), int(bool(layered)), max_iterations,
+                  PRECISIONS[precision], device)
+        h = C.c_void_p()
+        _check(lib().cb_code_create(C.byref(d), C.byref(h)))
+        self._h = h
+        info = np.zeros(16, np.int64)
+        _check(lib().cb_code_info(h, _p(info)), h)
+        (self.bg, self.z, self.k_info, self.e, self.k_sys, self.n_full, self.n_rows, self.edges, self.ils,
+         self.max_degree, self.rv, self.qm, self.core_terms, self.map_is_offset, self.n_entries, _) = (
+            int(x) for x in info)
+        self.precision = precision
+        self.dtype = np.float64 if precision == "f64" else np.float32
+        self.rule, self.alpha, self.max_iterations = rule_l, alpha, max_iterations
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cb_code_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # reference accessors (nr/ldpc.rs:164-182)
+    def base_graph(self):
+        return self.bg
+
+    def lifting_size(self):
+        return self.z
+
+    @property
+    def k(self):
+        return self.k_info
+
+    @property
+    def n(self):
+        return self.e
+
+    def tables(self):
+        """(entries [n_entries x 3] = (layer, base column, shift), bit map [E])."""
+        ent = np.zeros((self.n_entries, 3), np.int32)
+        bm = np.zeros(self.e, np.int32)
+        _check(lib().cb_code_tables(self._h, _p(ent), _p(bm)), self._h)
+        return ent, bm
+
+    def bit_map(self):
+        return self.tables()[1]
+
+    def encode(self, info):
+        """BlockCode::encode_block of one block (K' bits) or of rows of blocks."""
+        u = np.ascontiguousarray(info, np.uint8)
+        single = u.ndim == 1
+        u2 = u.reshape(-1, self.k_info)
+        out = np.zeros((u2.shape[0], self.e), np.uint8)
+        _check(lib().cb_encode(self._h, _p(u2), u2.shape[0], _p(out)), self._h)
+        return out[0] if single else out
+
+    def _decode(self, llr, want_bits=True, want_app=False, want_iters=True):
+        x = np.ascontiguousarray(llr, self.dtype)
+        single = x.ndim == 1
+        x2 = x.reshape(-1, self.e)
+        n = x2.shape[0]
+        bits = np.zeros((n, (self.k_info + 7) // 8), np.uint8) if want_bits else None
+        app = np.zeros((n, self.k_info), self.dtype) if want_app else None
+        it = np.zeros(n, np.int32) if want_iters else None
+        _check(lib().cb_decode(self._h, _p(x2), n, _p(bits), _p(app), _p(it)), self._h)
+        if bits is not None:
+            bits = np.unpackbits(bits, axis=1, bitorder="little")[:, :self.k_info]
+        return single, bits, app, it
+
+    def decode(self, llr):
+        """BlockCode::decode_block: the K' hard decisions of E channel LLRs (rows batched)."""
+        single, bits, _, _ = self._decode(llr)
+        return bits[0] if single else bits
+
+    def decode_full(self, llr):
+        """(hard decisions, a posteriori LLRs of the K' info bits, iterations)."""
+        single, bits, app, it = self._decode(llr, want_app=True)
+        if single:
+            return bits[0], app[0], int(it[0])
+        return bits, app, it
+
+    def app(self, llr):
+        """SoftDecode::app: the a posteriori LLRs of the information bits."""
+        return self.decode_full(llr)[1]
+
+    def run_frames(self, seed, name, condition, first_frame, n_frames, ebn0_db, modulation=4):
+        """Per-frame (bit_errors, frame_error, iterations) of frames [first, first + n)."""
+        out = np.zeros(n_frames, FRAME_DTYPE)
+        nh = fnv1a64(name) if isinstance(name, (str, bytes)) else int(name)
+        _check(lib().cb_run_frames(self._h, modulation, seed, nh, condition, first_frame, n_frames, ebn0_db,
+                                   _p(out)), self._h)
+        return out
+
+    def generate_frames(self, seed, name, condition, first_frame, n_frames, ebn0_db, modulation=4):
+        """(channel LLRs [n x E], info bits [n x K']) exactly as run_frames draws them."""
+        llr = np.zeros((n_frames, self.e), self.dtype)
+        info = np.zeros((n_frames, self.k_info), np.uint8)
+        nh = fnv1a64(name) if isinstance(name, (str, bytes)) else int(name)
+        _check(lib().cb_generate_frames(self._h, modulation, seed, nh, condition, first_frame, n_frames, ebn0_db,
+                                        _p(llr), _p(info)), self._h)
+        return llr, info

@@ -1,0 +1,585 @@
+// The C ABI of include/comrs_gb300.h: code objects, device buffers, chunked launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/comrs_gb300.h"
+#include "code_host.h"
+#include "kernels.h"
+
+#define CB_VERSION_STRING "comrs_gb300 0.1.0 (sm_103a)"
+
+namespace {
+
+thread_local std::string g_thread_error;
+
+struct GenCache {
+  int m = 0, mbits = 0, n_pad = 0, bpc = 0, spc = 0;
+  double log_m = 0;
+  std::vector<double> points;  // 2m
+  double* d_points = nullptr;
+  uint64_t* d_jumps = nullptr;
+};
+
+// Gray square QAM of order m, unit average energy (crates/com-mapping/src/
+// constellation.rs:168-202 with normalized, :396): natural row-major snake points,
+// label gray(i) for the i-th one, scaled by 1/sqrt(mean energy).
+bool qam_points(int m, std::vector<double>& pts, double& log_m) {
+  int side = (int)std::lround(std::sqrt((double)m));
+  if (m < 4 || (m & (m - 1)) || side * side != m || m > 256) return false;
+  std::vector<double> lv(side), nre, nim;
+  for (int i = 0; i < side; i++) lv[i] = 2.0 * (double)i - ((double)side - 1.0);
+  for (int r = 0; r < side; r++)
+    for (int t = 0; t < side; t++) {
+      int tt = (r % 2 == 1) ? side - 1 - t : t;
+      nre.push_back(lv[tt]);
+      nim.push_back(lv[side - 1 - r]);
+    }
+  pts.assign(2 * m, 0.0);
+  for (int i = 0; i < m; i++) {
+    int g = i ^ (i >> 1);
+    pts[2 * g] = nre[i];
+    pts[2 * g + 1] = nim[i];
+  }
+  double e = 0.0;
+  for (int i = 0; i < m; i++) e += pts[2 * i] * pts[2 * i] + pts[2 * i + 1] * pts[2 * i + 1];
+  double s = 1.0 / std::sqrt(e / (double)m);
+  for (double& v : pts) v *= s;
+  log_m = std::log((double)m);
+  return true;
+}
+
+}  // namespace
+
+struct cb_code {
+  std::mutex mu;
+  int device = 0;
+  int precision = 0;
+  cbh::NrCode host;
+  cbd::DevCode dev;
+  cbd::DecCfg cfg;
+  int32_t* d_map = nullptr;
+  int32_t* d_inv_start = nullptr;
+  int32_t* d_inv_t = nullptr;
+  void* d_state = nullptr;
+  int decode_grid = 0;
+  unsigned long long* d_counter = nullptr;
+  int32_t* d_status = nullptr;
+  cudaStream_t stream = nullptr;
+  // scratch, grown on demand
+  void* d_llr = nullptr;
+  size_t llr_cap = 0;
+  uint32_t* d_bits = nullptr;
+  size_t bits_cap = 0;
+  uint32_t* d_info = nullptr;
+  size_t info_cap = 0;
+  void* d_app = nullptr;
+  size_t app_cap = 0;
+  int32_t* d_iters = nullptr;
+  size_t iters_cap = 0;
+  cbd::FrameResult* d_results = nullptr;
+  size_t results_cap = 0;
+  uint8_t* d_u8 = nullptr;
+  size_t u8_cap = 0;
+  std::vector<uint32_t> h_words;
+  std::map<int, GenCache> gen;
+  bool dev_ready = false;
+  std::string err;
+};
+
+namespace {
+
+cb_status fail(cb_code* c, cb_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  g_thread_error = msg;
+  return s;
+}
+
+cb_status cuda_fail(cb_code* c, cudaError_t e, const char* what) {
+  return fail(c, CB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CB_CUDA(c, call)                                   \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail((c), e_, #call); \
+  } while (0)
+
+template <typename P>
+cudaError_t grow(P*& ptr, size_t& cap, size_t bytes) {
+  if (bytes <= cap) return cudaSuccess;
+  if (ptr) cudaFree((void*)ptr);
+  ptr = nullptr;
+  cap = 0;
+  size_t want = std::max(bytes, cap * 3 / 2);
+  cudaError_t e = cudaMalloc((void**)&ptr, want);
+  if (e == cudaSuccess) cap = want;
+  return e;
+}
+
+size_t elem_size(const cb_code* c) { return c->precision == CB_F64 ? sizeof(double) : sizeof(float); }
+
+// frames per launch chunk: bounded so the scratch stays a few hundred MB
+int64_t chunk_frames(const cb_code* c) {
+  size_t per = (size_t)c->host.e * elem_size(c) + 64;
+  int64_t n = (int64_t)((size_t)512 << 20) / (int64_t)per;
+  return std::max<int64_t>(1, std::min<int64_t>(n, 65536));
+}
+
+template <typename T>
+cb_status decode_device_impl(cb_code* c, const T* llr, int64_t n, uint32_t* bits, T* app, int32_t* iters,
+                             const uint32_t* ref, cbd::FrameResult* results, cudaStream_t s) {
+  cbk::DecodeArgs<T> a;
+  a.code = c->dev;
+  a.cfg = c->cfg;
+  a.llr = llr;
+  a.n_frames = n;
+  a.bits_out = bits;
+  a.app_out = app;
+  a.post_out = nullptr;
+  a.iters_out = iters;
+  a.ref_bits = ref;
+  a.results = results;
+  a.state = reinterpret_cast<T*>(c->d_state);
+  a.work_counter = reinterpret_cast<int32_t*>(c->d_counter);
+  a.status = c->d_status;
+  CB_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), s));
+  int grid = (int)std::min<int64_t>(c->decode_grid, n);
+  CB_CUDA(c, cbk::launch_decode<T>(a, grid, s));
+  return CB_OK;
+}
+
+cb_status gen_config(cb_code* c, int m, GenCache** out) {
+  auto it = c->gen.find(m);
+  if (it != c->gen.end()) { *out = &it->second; return CB_OK; }
+  GenCache g;
+  if (!qam_points(m, g.points, g.log_m)) return fail(c, CB_ERR_CONFIG, "modulation order must be 4, 16, 64 or 256");
+  g.m = m;
+  g.mbits = __builtin_ctz(m);
+  const int e = c->host.e, k = c->host.k_info, NT = cbk::kGenThreads;
+  g.n_pad = (g.mbits - e % g.mbits) % g.mbits;
+  int n_sym = (e + g.n_pad) / g.mbits;
+  g.bpc = (k + NT - 1) / NT;
+  g.spc = (n_sym + NT - 1) / NT;
+  std::vector<uint64_t> polys((size_t)(2 * NT + 1) * 4);
+  cbh::JumpPoly step_b = cbh::xoshiro_jump_poly((uint64_t)g.bpc), cur = cbh::xoshiro_jump_poly(0);
+  for (int t = 0; t < NT; t++) {
+    std::memcpy(&polys[(size_t)t * 4], cur.w, 32);
+    cur = cbh::xoshiro_jump_mul(cur, step_b);
+  }
+  cbh::JumpPoly step_s = cbh::xoshiro_jump_poly(2ull * g.spc);
+  cur = cbh::xoshiro_jump_poly((uint64_t)k + g.n_pad);
+  for (int t = 0; t < NT; t++) {
+    std::memcpy(&polys[(size_t)(NT + t) * 4], cur.w, 32);
+    cur = cbh::xoshiro_jump_mul(cur, step_s);
+  }
+  cbh::JumpPoly padp = cbh::xoshiro_jump_poly((uint64_t)k);
+  std::memcpy(&polys[(size_t)(2 * NT) * 4], padp.w, 32);
+  CB_CUDA(c, cudaMalloc(&g.d_points, sizeof(double) * 2 * m));
+  CB_CUDA(c, cudaMemcpy(g.d_points, g.points.data(), sizeof(double) * 2 * m, cudaMemcpyHostToDevice));
+  CB_CUDA(c, cudaMalloc(&g.d_jumps, polys.size() * 8));
+  CB_CUDA(c, cudaMemcpy(g.d_jumps, polys.data(), polys.size() * 8, cudaMemcpyHostToDevice));
+  auto res = c->gen.emplace(m, g);
+  *out = &res.first->second;
+  return CB_OK;
+}
+
+template <typename T>
+cb_status gen_device(cb_code* c, GenCache* g, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first,
+                     int64_t n, double ebn0_db, T* llr, uint32_t* info, cudaStream_t s) {
+  cbk::GenArgs<T> a;
+  a.code = c->dev;
+  a.m = g->m;
+  a.mbits = g->mbits;
+  a.points = g->d_points;
+  a.log_m = g->log_m;
+  // b = log2 M * R (com-spec blocks/channel.rs:145-149), times db2lin (units.rs:38-40)
+  double rate = (double)c->host.k_info / (double)c->host.e;
+  double b = (double)g->mbits * rate;
+  a.b_ebn0 = b * std::pow(10.0, ebn0_db / 10.0);
+  a.seed = seed;
+  a.name_hash = name_hash;
+  a.cond = cond;
+  a.first_frame = first;
+  a.n_frames = n;
+  a.jumps = g->d_jumps;
+  a.bits_per_chunk = g->bpc;
+  a.syms_per_chunk = g->spc;
+  a.n_pad = g->n_pad;
+  a.llr_out = llr;
+  a.info_out = info;
+  CB_CUDA(c, cbk::launch_gen<T>(a, s));
+  return CB_OK;
+}
+
+template <typename T>
+cb_status run_frames_impl(cb_code* c, int m, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first,
+                          int64_t n, double ebn0_db, cb_frame_result* out, void* llr_host, uint8_t* info_host) {
+  GenCache* g;
+  cb_status st = gen_config(c, m, &g);
+  if (st) return st;
+  const int wpf = (c->host.k_info + 31) / 32;
+  const int64_t chunk = chunk_frames(c);
+  for (int64_t done = 0; done < n; done += chunk) {
+    int64_t cnt = std::min(chunk, n - done);
+    CB_CUDA(c, grow(c->d_llr, c->llr_cap, (size_t)cnt * c->host.e * sizeof(T)));
+    CB_CUDA(c, grow(c->d_info, c->info_cap, (size_t)cnt * wpf * 4));
+    CB_CUDA(c, grow(c->d_results, c->results_cap, (size_t)cnt * sizeof(cbd::FrameResult)));
+    T* llr = reinterpret_cast<T*>(c->d_llr);
+    st = gen_device<T>(c, g, seed, name_hash, cond, first + (uint64_t)done, cnt, ebn0_db, llr, c->d_info, c->stream);
+    if (st) return st;
+    if (out) {
+      st = decode_device_impl<T>(c, llr, cnt, nullptr, nullptr, nullptr, c->d_info, c->d_results, c->stream);
+      if (st) return st;
+      CB_CUDA(c, cudaMemcpyAsync(out + done, c->d_results, (size_t)cnt * sizeof(cb_frame_result),
+                                 cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (llr_host)
+      CB_CUDA(c, cudaMemcpyAsync(reinterpret_cast<T*>(llr_host) + (size_t)done * c->host.e, llr,
+                                 (size_t)cnt * c->host.e * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+    if (info_host) {
+      c->h_words.resize((size_t)cnt * wpf);
+      CB_CUDA(c, cudaMemcpyAsync(c->h_words.data(), c->d_info, (size_t)cnt * wpf * 4, cudaMemcpyDeviceToHost,
+                                 c->stream));
+      CB_CUDA(c, cudaStreamSynchronize(c->stream));
+      for (int64_t f = 0; f < cnt; f++)
+        for (int i = 0; i < c->host.k_info; i++)
+          info_host[(size_t)(done + f) * c->host.k_info + i] =
+              (uint8_t)((c->h_words[(size_t)f * wpf + i / 32] >> (i % 32)) & 1u);
+    }
+  }
+  CB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CB_OK;
+}
+
+// frames on a caller stream: results (and optionally the LLRs / info words) in device
+// memory; the LLRs go to the caller's buffer or to the code's scratch
+template <typename T>
+cb_status trial_device_impl(cb_code* c, int m, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first,
+                            int64_t n, double ebn0_db, cbd::FrameResult* results, T* llr_dev, uint32_t* info_dev,
+                            cudaStream_t s) {
+  GenCache* g;
+  cb_status st = gen_config(c, m, &g);
+  if (st) return st;
+  const int wpf = (c->host.k_info + 31) / 32;
+  if (!llr_dev) {
+    CB_CUDA(c, grow(c->d_llr, c->llr_cap, (size_t)n * c->host.e * sizeof(T)));
+    llr_dev = reinterpret_cast<T*>(c->d_llr);
+  }
+  if (!info_dev) {
+    CB_CUDA(c, grow(c->d_info, c->info_cap, (size_t)n * wpf * 4));
+    info_dev = c->d_info;
+  }
+  st = gen_device<T>(c, g, seed, name_hash, cond, first, n, ebn0_db, llr_dev, info_dev, s);
+  if (st || !results) return st;
+  return decode_device_impl<T>(c, llr_dev, n, nullptr, nullptr, nullptr, info_dev, results, s);
+}
+
+template <typename T>
+cb_status decode_host_impl(cb_code* c, const T* llr, int64_t n, uint8_t* bits, T* app, int32_t* iters) {
+  const int wpf = (c->host.k_info + 31) / 32;
+  const int bpf = (c->host.k_info + 7) / 8;
+  const int64_t chunk = chunk_frames(c);
+  for (int64_t done = 0; done < n; done += chunk) {
+    int64_t cnt = std::min(chunk, n - done);
+    CB_CUDA(c, grow(c->d_llr, c->llr_cap, (size_t)cnt * c->host.e * sizeof(T)));
+    CB_CUDA(c, grow(c->d_bits, c->bits_cap, (size_t)cnt * wpf * 4));
+    if (app) CB_CUDA(c, grow(c->d_app, c->app_cap, (size_t)cnt * c->host.k_info * sizeof(T)));
+    if (iters) CB_CUDA(c, grow(c->d_iters, c->iters_cap, (size_t)cnt * 4));
+    T* d_llr = reinterpret_cast<T*>(c->d_llr);
+    CB_CUDA(c, cudaMemcpyAsync(d_llr, llr + (size_t)done * c->host.e, (size_t)cnt * c->host.e * sizeof(T),
+                               cudaMemcpyHostToDevice, c->stream));
+    cb_status st = decode_device_impl<T>(c, d_llr, cnt, c->d_bits, app ? reinterpret_cast<T*>(c->d_app) : nullptr,
+                                         iters ? c->d_iters : nullptr, nullptr, nullptr, c->stream);
+    if (st) return st;
+    if (bits) {
+      if (bpf == wpf * 4) {
+        CB_CUDA(c, cudaMemcpyAsync(bits + (size_t)done * bpf, c->d_bits, (size_t)cnt * bpf, cudaMemcpyDeviceToHost,
+                                   c->stream));
+      } else {
+        c->h_words.resize((size_t)cnt * wpf);
+        CB_CUDA(c, cudaMemcpyAsync(c->h_words.data(), c->d_bits, (size_t)cnt * wpf * 4, cudaMemcpyDeviceToHost,
+                                   c->stream));
+        CB_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int64_t f = 0; f < cnt; f++)
+          std::memcpy(bits + (size_t)(done + f) * bpf, &c->h_words[(size_t)f * wpf], bpf);
+      }
+    }
+    if (app)
+      CB_CUDA(c, cudaMemcpyAsync(app + (size_t)done * c->host.k_info, c->d_app,
+                                 (size_t)cnt * c->host.k_info * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+    if (iters)
+      CB_CUDA(c, cudaMemcpyAsync(iters + done, c->d_iters, (size_t)cnt * 4, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CB_OK;
+}
+
+
+// Device resources are created on first use, so that a code object (its tables and the
+// host encoder) also exists on a machine without a GPU.
+cb_status ensure_device(cb_code* c) {
+  if (c->dev_ready) return CB_OK;
+  const cbh::NrCode& h = c->host;
+  cbd::DevCode& v = c->dev;
+  CB_CUDA(c, cudaSetDevice(c->device));
+  CB_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CB_CUDA(c, cudaMalloc(&c->d_map, sizeof(int32_t) * h.e));
+  CB_CUDA(c, cudaMemcpy(c->d_map, h.map.data(), sizeof(int32_t) * h.e, cudaMemcpyHostToDevice));
+  CB_CUDA(c, cudaMalloc(&c->d_inv_start, sizeof(int32_t) * (h.n_full + 1)));
+  CB_CUDA(c, cudaMemcpy(c->d_inv_start, h.inv_start.data(), sizeof(int32_t) * (h.n_full + 1), cudaMemcpyHostToDevice));
+  CB_CUDA(c, cudaMalloc(&c->d_inv_t, sizeof(int32_t) * h.e));
+  CB_CUDA(c, cudaMemcpy(c->d_inv_t, h.inv_t.data(), sizeof(int32_t) * h.e, cudaMemcpyHostToDevice));
+  CB_CUDA(c, cudaMalloc(&c->d_counter, 64));
+  CB_CUDA(c, cudaMalloc(&c->d_status, 64));
+  CB_CUDA(c, cudaMemset(c->d_status, 0, 64));
+  v.map = c->d_map;
+  v.inv_start = c->d_inv_start;
+  v.inv_t = c->d_inv_t;
+  c->decode_grid = cbk::decode_grid_size(v, c->precision, c->device);
+  if (c->decode_grid <= 0) return fail(c, CB_ERR_CUDA, "the decoder does not fit an SM (occupancy 0)");
+  CB_CUDA(c, cudaMalloc(&c->d_state, cbk::decode_state_bytes_per_slot(v, c->precision) * c->decode_grid));
+  c->dev_ready = true;
+  return CB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cb_version(void) { return CB_VERSION_STRING; }
+
+const char* cb_last_error(const cb_code* c) { return c ? c->err.c_str() : g_thread_error.c_str(); }
+
+cb_status cb_code_create(const cb_code_desc* d, cb_code** out) {
+  if (!out) return fail(nullptr, CB_ERR_CONFIG, "out is NULL");
+  *out = nullptr;
+  if (!d) return fail(nullptr, CB_ERR_CONFIG, "desc is NULL");
+  if (d->precision != CB_F64 && d->precision != CB_F32) return fail(nullptr, CB_ERR_CONFIG, "precision is 0 or 1");
+  if (d->rule != CB_RULE_NMS && d->rule != CB_RULE_OMS)
+    return fail(nullptr, CB_ERR_CONFIG, "the GPU decoder implements normalized_min_sum and offset_min_sum");
+  if (!d->layered) return fail(nullptr, CB_ERR_CONFIG, "the GPU decoder implements the layered schedule");
+  if (d->max_iterations < 0 || d->max_iterations > 255) return fail(nullptr, CB_ERR_CONFIG, "max_iterations in 0..255");
+  if (!(std::isfinite(d->alpha))) return fail(nullptr, CB_ERR_CONFIG, "alpha must be finite");
+  cbh::CodeSpec spec;
+  spec.k_info = d->k_info;
+  spec.e = d->e;
+  spec.bg = d->base_graph;
+  spec.z = d->lifting_size;
+  spec.rv = d->rv;
+  spec.qm = d->qm;
+  cb_code* c = new cb_code();
+  std::string err;
+  if (!cbh::build_nr_code(spec, c->host, err)) {
+    delete c;
+    return fail(nullptr, CB_ERR_CONFIG, err);
+  }
+  c->device = d->device;
+  c->precision = d->precision;
+  c->cfg.rule = d->rule;
+  c->cfg.alpha = d->alpha;
+  c->cfg.layered = d->layered;
+  c->cfg.max_iterations = d->max_iterations;
+  const cbh::NrCode& h = c->host;
+  cbd::DevCode& v = c->dev;
+  std::memset(&v, 0, sizeof v);
+  v.bg = h.bg;
+  v.z = h.z;
+  v.cols_k = h.cols_k;
+  v.rows_n = h.rows_n;
+  v.n_full = h.n_full;
+  v.k = h.k;
+  v.k_info = h.k_info;
+  v.e = h.e;
+  v.qm = h.qm;
+  v.max_degree = h.max_degree;
+  v.n_entries = (int)h.entry_col.size();
+  v.n_core_terms = (int)h.core_terms.size();
+  v.map_is_offset = h.map_is_offset;
+  v.has_repeats = h.has_repeats;
+  for (int i = 0; i <= h.rows_n; i++) v.layer_start[i] = (uint16_t)h.layer_start[i];
+  for (int t = 0; t < v.n_entries; t++) v.entry[t] = ((uint32_t)h.entry_col[t] << 16) | h.entry_shift[t];
+  for (int t = 0; t < v.n_core_terms; t++)
+    v.core_term[t] = ((uint32_t)h.core_terms[t].block << 20) | ((uint32_t)h.core_terms[t].src << 16) |
+                     h.core_terms[t].shift;
+  *out = c;
+  return CB_OK;
+}
+
+void cb_code_destroy(cb_code* c) {
+  if (!c) return;
+  if (c->dev_ready || c->stream) cudaSetDevice(c->device);
+  for (auto& kv : c->gen) {
+    cudaFree(kv.second.d_points);
+    cudaFree(kv.second.d_jumps);
+  }
+  void* bufs[] = {c->d_map, c->d_inv_start, c->d_inv_t, c->d_state, c->d_counter, c->d_status, c->d_llr, c->d_bits,
+                  c->d_info, c->d_app, c->d_iters, c->d_results, c->d_u8};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+cb_status cb_code_info(const cb_code* c, int64_t info[16]) {
+  if (!c || !info) return fail(nullptr, CB_ERR_CONFIG, "NULL argument");
+  const cbh::NrCode& h = c->host;
+  int64_t v[16] = {h.bg, h.z, h.k_info, h.e, h.k, h.n_full, (int64_t)h.rows_n * h.z, h.edges, h.ils, h.max_degree,
+                   h.rv, h.qm, (int64_t)h.core_terms.size(), h.map_is_offset ? 1 : 0, (int64_t)h.entry_col.size(), 0};
+  std::memcpy(info, v, sizeof v);
+  return CB_OK;
+}
+
+cb_status cb_code_tables(const cb_code* c, int32_t* entries, int32_t* bit_map) {
+  if (!c) return fail(nullptr, CB_ERR_CONFIG, "NULL code");
+  const cbh::NrCode& h = c->host;
+  if (entries) {
+    int t = 0;
+    for (int L = 0; L < h.rows_n; L++)
+      for (int i = h.layer_start[L]; i < h.layer_start[L + 1]; i++, t++) {
+        entries[3 * t] = L;
+        entries[3 * t + 1] = h.entry_col[i];
+        entries[3 * t + 2] = h.entry_shift[i];
+      }
+  }
+  if (bit_map) std::memcpy(bit_map, h.map.data(), sizeof(int32_t) * h.e);
+  return CB_OK;
+}
+
+cb_status cb_encode(cb_code* c, const uint8_t* info, int64_t n, uint8_t* out) {
+  if (!c || !info || !out || n < 0) return fail(c, CB_ERR_CONFIG, "NULL argument or negative count");
+  std::lock_guard<std::mutex> lock(c->mu);
+  // host encoder over the same construction tables (the GPU encoder lives inside the
+  // frame generator, where the bits are drawn)
+  const cbh::NrCode& h = c->host;
+  std::vector<uint8_t> cw(h.n_full), syn(4 * h.z);
+  for (int64_t f = 0; f < n; f++) {
+    std::fill(cw.begin(), cw.end(), 0);
+    for (int i = 0; i < h.k_info; i++) cw[i] = info[(size_t)f * h.k_info + i] & 1;
+    for (int L = 0; L < 4; L++)
+      for (int r = 0; r < h.z; r++) {
+        uint8_t a = 0;
+        for (int t = h.layer_start[L]; t < h.layer_start[L + 1]; t++)
+          if (h.entry_col[t] < h.cols_k) a ^= cw[h.entry_col[t] * h.z + (r + h.entry_shift[t]) % h.z];
+        syn[L * h.z + r] = a;
+      }
+    for (int blk = 0; blk < 4; blk++)
+      for (int r = 0; r < h.z; r++) {
+        uint8_t a = 0;
+        for (auto& ct : h.core_terms)
+          if (ct.block == blk) a ^= syn[ct.src * h.z + (r + ct.shift) % h.z];
+        cw[h.k + blk * h.z + r] = a;
+      }
+    for (int L = 4; L < h.rows_n; L++)
+      for (int r = 0; r < h.z; r++) {
+        int own = h.k + L * h.z + r;
+        uint8_t a = 0;
+        for (int t = h.layer_start[L]; t < h.layer_start[L + 1]; t++) {
+          int col = h.entry_col[t] * h.z + (r + h.entry_shift[t]) % h.z;
+          if (col != own) a ^= cw[col];
+        }
+        cw[own] = a;
+      }
+    for (int t = 0; t < h.e; t++) out[(size_t)f * h.e + t] = cw[h.map[t]];
+  }
+  return CB_OK;
+}
+
+cb_status cb_decode(cb_code* c, const void* llr, int64_t n, uint8_t* bits, void* app, int32_t* iters) {
+  if (!c || !llr || n < 0) return fail(c, CB_ERR_CONFIG, "NULL argument or negative count");
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (cb_status st = ensure_device(c)) return st;
+  if (n == 0) return CB_OK;
+  if (c->precision == CB_F64)
+    return decode_host_impl<double>(c, (const double*)llr, n, bits, (double*)app, iters);
+  return decode_host_impl<float>(c, (const float*)llr, n, bits, (float*)app, iters);
+}
+
+cb_status cb_decode_device(cb_code* c, const void* llr, int64_t n, uint32_t* bits, void* app, int32_t* iters,
+                           void* stream) {
+  if (!c || !llr || n < 0) return fail(c, CB_ERR_CONFIG, "NULL argument or negative count");
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (cb_status st = ensure_device(c)) return st;
+  if (n == 0) return CB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (c->precision == CB_F64)
+    return decode_device_impl<double>(c, (const double*)llr, n, bits, (double*)app, iters, nullptr, nullptr, s);
+  return decode_device_impl<float>(c, (const float*)llr, n, bits, (float*)app, iters, nullptr, nullptr, s);
+}
+
+cb_status cb_run_frames(cb_code* c, int32_t m, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first,
+                        int64_t n, double ebn0_db, cb_frame_result* out) {
+  if (!c || !out || n < 0) return fail(c, CB_ERR_CONFIG, "NULL argument or negative count");
+  if (!std::isfinite(ebn0_db)) return fail(c, CB_ERR_CONFIG, "Eb/N0 must be finite");
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (cb_status st = ensure_device(c)) return st;
+  if (n == 0) return CB_OK;
+  if (c->precision == CB_F64)
+    return run_frames_impl<double>(c, m, seed, name_hash, cond, first, n, ebn0_db, out, nullptr, nullptr);
+  return run_frames_impl<float>(c, m, seed, name_hash, cond, first, n, ebn0_db, out, nullptr, nullptr);
+}
+
+cb_status cb_generate_frames(cb_code* c, int32_t m, uint64_t seed, uint64_t name_hash, uint64_t cond,
+                             uint64_t first, int64_t n, double ebn0_db, void* llr, uint8_t* info) {
+  if (!c || n < 0) return fail(c, CB_ERR_CONFIG, "NULL argument or negative count");
+  if (!std::isfinite(ebn0_db)) return fail(c, CB_ERR_CONFIG, "Eb/N0 must be finite");
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (cb_status st = ensure_device(c)) return st;
+  if (n == 0) return CB_OK;
+  if (c->precision == CB_F64)
+    return run_frames_impl<double>(c, m, seed, name_hash, cond, first, n, ebn0_db, nullptr, llr, info);
+  return run_frames_impl<float>(c, m, seed, name_hash, cond, first, n, ebn0_db, nullptr, llr, info);
+}
+
+cb_status cb_run_frames_device(cb_code* c, int32_t m, uint64_t seed, uint64_t name_hash, uint64_t cond,
+                               uint64_t first, int64_t n, double ebn0_db, cb_frame_result* results_dev, void* stream) {
+  if (!c || !results_dev || n < 0) return fail(c, CB_ERR_CONFIG, "NULL argument or negative count");
+  if (!std::isfinite(ebn0_db)) return fail(c, CB_ERR_CONFIG, "Eb/N0 must be finite");
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (cb_status st = ensure_device(c)) return st;
+  if (n == 0) return CB_OK;
+  cbd::FrameResult* r = reinterpret_cast<cbd::FrameResult*>(results_dev);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (c->precision == CB_F64)
+    return trial_device_impl<double>(c, m, seed, name_hash, cond, first, n, ebn0_db, r, nullptr, nullptr, s);
+  return trial_device_impl<float>(c, m, seed, name_hash, cond, first, n, ebn0_db, r, nullptr, nullptr, s);
+}
+
+cb_status cb_generate_frames_device(cb_code* c, int32_t m, uint64_t seed, uint64_t name_hash, uint64_t cond,
+                                    uint64_t first, int64_t n, double ebn0_db, void* llr_dev, uint32_t* info_dev,
+                                    void* stream) {
+  if (!c || !llr_dev || !info_dev || n < 0) return fail(c, CB_ERR_CONFIG, "NULL argument or negative count");
+  if (!std::isfinite(ebn0_db)) return fail(c, CB_ERR_CONFIG, "Eb/N0 must be finite");
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (cb_status st = ensure_device(c)) return st;
+  if (n == 0) return CB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (c->precision == CB_F64)
+    return trial_device_impl<double>(c, m, seed, name_hash, cond, first, n, ebn0_db, nullptr, (double*)llr_dev,
+                                     info_dev, s);
+  return trial_device_impl<float>(c, m, seed, name_hash, cond, first, n, ebn0_db, nullptr, (float*)llr_dev,
+                                  info_dev, s);
+}
+
+cb_status cb_xoshiro_jump(const uint64_t state[4], uint64_t steps, uint64_t out[4]) {
+  if (!state || !out) return fail(nullptr, CB_ERR_CONFIG, "NULL argument");
+  uint64_t s[4] = {state[0], state[1], state[2], state[3]};
+  cbh::xoshiro_apply_jump(s, cbh::xoshiro_jump_poly(steps));
+  std::memcpy(out, s, sizeof s);
+  return CB_OK;
+}
+
+}  // extern "C"

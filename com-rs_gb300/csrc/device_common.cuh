@@ -1,0 +1,117 @@
+// Shared device-side pieces: the per-frame xoshiro256** streams, the code descriptor
+// handed to every kernel, and the per-frame result record.
+#pragma once
+#include <cstdint>
+
+#include "code_host.h"
+
+namespace cbd {
+
+// ---------------------------------------------------------------- xoshiro256**
+// crates/com-core/src/rng.rs:49-117, :270-278 (bit-identical)
+struct Xoshiro {
+  uint64_t s0, s1, s2, s3;
+};
+
+__host__ __device__ __forceinline__ uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t& st) {
+  st += 0x9E3779B97F4A7C15ull;
+  uint64_t z = st;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__host__ __device__ __forceinline__ Xoshiro xoshiro_seed(uint64_t seed) {
+  Xoshiro r;
+  uint64_t st = seed;
+  r.s0 = splitmix64(st);
+  r.s1 = splitmix64(st);
+  r.s2 = splitmix64(st);
+  r.s3 = splitmix64(st);
+  return r;
+}
+
+// stream(base_seed, experiment, condition, trial) with the experiment already hashed
+__host__ __device__ __forceinline__ Xoshiro stream(uint64_t base_seed, uint64_t name_hash, uint64_t cond,
+                                                   uint64_t trial) {
+  uint64_t st = base_seed ^ name_hash;
+  uint64_t a = splitmix64(st);
+  st = a ^ cond;
+  uint64_t b = splitmix64(st);
+  st = b ^ trial;
+  return xoshiro_seed(splitmix64(st));
+}
+
+__host__ __device__ __forceinline__ void xoshiro_advance(Xoshiro& r) {
+  uint64_t t = r.s1 << 17;
+  r.s2 ^= r.s0;
+  r.s3 ^= r.s1;
+  r.s1 ^= r.s2;
+  r.s0 ^= r.s3;
+  r.s2 ^= t;
+  r.s3 = rotl64(r.s3, 45);
+}
+
+__host__ __device__ __forceinline__ uint64_t xoshiro_next(Xoshiro& r) {
+  uint64_t result = rotl64(r.s1 * 5, 7) * 9;
+  xoshiro_advance(r);
+  return result;
+}
+
+// state after n steps, n given by its jump polynomial x^n mod P(x)
+__device__ __forceinline__ void xoshiro_jump(Xoshiro& r, const uint64_t* poly) {
+  uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll 1
+  for (int w = 0; w < 4; w++) {
+    uint64_t bits = poly[w];
+#pragma unroll 4
+    for (int b = 0; b < 64; b++) {
+      uint64_t mask = 0ull - ((bits >> b) & 1ull);
+      a0 ^= r.s0 & mask;
+      a1 ^= r.s1 & mask;
+      a2 ^= r.s2 & mask;
+      a3 ^= r.s3 & mask;
+      xoshiro_advance(r);
+    }
+  }
+  r.s0 = a0;
+  r.s1 = a1;
+  r.s2 = a2;
+  r.s3 = a3;
+}
+
+// ---------------------------------------------------------------- code descriptor
+struct DevCode {
+  int32_t bg, z, cols_k, rows_n, n_full, k, k_info, e, qm;
+  int32_t max_degree, n_entries, n_core_terms;
+  int32_t map_is_offset, has_repeats;
+  const int32_t* map;        // E positions (device), unused when map_is_offset
+  const int32_t* inv_start;  // n_full + 1 (device), when !map_is_offset
+  const int32_t* inv_t;      // E (device)
+  uint16_t layer_start[cbh::kMaxLayers + 1];
+  uint32_t entry[cbh::kMaxEntries];      // (base column << 16) | shift
+  uint32_t core_term[cbh::kMaxCoreTerms];  // (block << 20) | (src << 16) | shift
+};
+
+// decoder settings (crates/com-fec/src/ldpc.rs:165-172)
+enum RuleId { RULE_SUM_PRODUCT = 0, RULE_NMS = 1, RULE_OMS = 2 };
+struct DecCfg {
+  int32_t rule;
+  int32_t max_iterations;
+  int32_t layered;
+  double alpha;  // scale of the NMS or offset of the OMS
+};
+
+// per-frame result record: bit errors, frame error, iterations
+struct FrameResult {
+  uint32_t bit_errors;
+  uint8_t frame_error;
+  uint8_t iterations;
+  uint16_t reserved;
+};
+
+constexpr float kKnownBitLlr = 30.0f;  // KNOWN_BIT_LLR, crates/com-core/src/signal.rs:37
+
+}  // namespace cbd

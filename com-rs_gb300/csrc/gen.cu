@@ -1,0 +1,254 @@
+// One BICM-LDPC frame per CTA: info bits, NR encoding, rate matching, Gray QAM
+// mapping, measured-power AWGN and max-log LLRs, regenerated on the device from the
+// frame's stream(seed, name, condition, frame) exactly as the reference draws them.
+//
+// Draw order of a frame (the spec chain of com-spec): K' bits, one next_u64 each
+// (source::bits, crates/com-mapping/src/source.rs:30-32, Rng::bit rng.rs:146-148); the
+// padding bits of map (blocks/coding/map.rs:36-38); then two uniforms per symbol for
+// its complex Gaussian (rng.rs:161-167).  The draws are split over the CTA's threads in
+// contiguous chunks; each thread reaches its chunk's start with a xoshiro256**
+// jump-ahead polynomial (the state after n steps is P_n(T) s, P_n = x^n mod the
+// characteristic polynomial of the transition T), so every value equals the
+// sequential draw.
+//
+// Encoding: LdpcCode::encode_block with Encoder::Core (crates/com-fec/src/ldpc.rs:
+// 774-786): the syndromes of the four core base rows, the core parity from the
+// block-circulant inverse of the core (computed on the host), then every extension
+// parity bit from its own row.  Rate matching is BitSelection::select
+// (crates/com-fec/src/puncture.rs:144-148) over the positions of nr/ldpc.rs:135-160.
+//
+// Channel and demapper:
+//   sigma^2 = P_meas / (log2 M * R * 10^(Eb/N0 / 10))  (crates/com-channel/src/awgn.rs:
+//   139-141, com-spec blocks/channel.rs:141-156, P_meas = the mean power of the frame's
+//   symbols summed in symbol order, blocks/frame.rs:256-259);
+//   y = x + sqrt(sigma^2) * CN(0, 1)  (awgn.rs:94-99);
+//   L_b = max_{i: b=0} metric_i - max_{i: b=1} metric_i, metric_i = -|y - x_i|^2 /
+//   sigma^2 - ln M  (crates/com-mapping/src/demapper.rs:82-146, :270-297).
+// f64 frames compute all of it in f64 with the correctly-rounded log/sin/cos of
+// crmath.cuh: bit-identical to the reference's draws up to the platform libm's last
+// bit.  f32 frames draw the same bits and the same uniforms, take the Gaussian in f32
+// and the max-log LLRs per I/Q dimension (the Gray square QAM labels split into an
+// imaginary-part and a real-part Gray code, so the max-log LLRs separate exactly).
+#include <cuda_runtime.h>
+
+#include "crmath.cuh"
+#include "kernels.h"
+
+namespace cbk {
+namespace {
+
+constexpr int NT = kGenThreads;
+
+__device__ __forceinline__ int gray(int i) { return i ^ (i >> 1); }
+
+template <typename T>
+__global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const cbd::DevCode& c = a.code;
+  const int z = c.z, tid = threadIdx.x;
+  const int n_sym = (c.e + a.n_pad) / a.mbits;
+  // shared layout: points (2M doubles) | syndromes (4Z) | codeword (n_full) | labels
+  double* pts = reinterpret_cast<double*>(smem);
+  uint8_t* syn = reinterpret_cast<uint8_t*>(pts + 2 * a.m);
+  uint8_t* cw = syn + 4 * z;
+  uint8_t* lab = cw + c.n_full;
+  uint8_t* pad = lab + n_sym;  // padding bits (< mbits)
+  __shared__ double s_sigma2;
+  const long long frame = (long long)blockIdx.x;
+  if (frame >= a.n_frames) return;
+  const uint64_t fidx = a.first_frame + (uint64_t)frame;
+
+  for (int i = tid; i < 2 * a.m; i += NT) pts[i] = a.points[i];
+  // ---- info bits: chunk [tid * bpc, (tid + 1) * bpc)
+  {
+    cbd::Xoshiro r = cbd::stream(a.seed, a.name_hash, a.cond, fidx);
+    int b0 = tid * a.bits_per_chunk, b1 = min(b0 + a.bits_per_chunk, c.k_info);
+    if (b0 < b1) {
+      cbd::xoshiro_jump(r, a.jumps + 4 * tid);
+      for (int i = b0; i < b1; i++) cw[i] = (uint8_t)(cbd::xoshiro_next(r) >> 63);
+    }
+    if (tid == 0 && a.n_pad) {  // the padding bits follow the info bits
+      cbd::Xoshiro p = cbd::stream(a.seed, a.name_hash, a.cond, fidx);
+      cbd::xoshiro_jump(p, a.jumps + 4 * (2 * NT));
+      for (int i = 0; i < a.n_pad; i++) pad[i] = (uint8_t)(cbd::xoshiro_next(p) >> 63);
+    }
+  }
+  for (int i = c.k_info + tid; i < c.n_full; i += NT) cw[i] = 0;
+  __syncthreads();
+  // packed info bits for the error counts
+  {
+    const int lane = tid & 31, warp = tid >> 5, wpf = (c.k_info + 31) >> 5;
+    for (int b0 = warp * 32; b0 < c.k_info; b0 += (NT / 32) * 32) {
+      int v = b0 + lane;
+      uint32_t word = __ballot_sync(0xffffffffu, v < c.k_info && cw[v]);
+      if (lane == 0) a.info_out[(size_t)frame * wpf + (b0 >> 5)] = word;
+    }
+  }
+  // ---- encoder: core syndromes over the systematic columns
+  for (int task = tid; task < 4 * z; task += NT) {
+    int L = task / z, r = task - L * z;
+    uint32_t acc = 0;
+    for (int t = c.layer_start[L]; t < c.layer_start[L + 1]; t++) {
+      uint32_t en = c.entry[t];
+      int j = (int)(en >> 16);
+      if (j >= c.cols_k) continue;
+      int cc = r + (int)(en & 0xffffu);
+      cc -= (cc >= z) ? z : 0;
+      acc ^= cw[j * z + cc];
+    }
+    syn[task] = (uint8_t)acc;
+  }
+  __syncthreads();
+  // core parity: block-circulant inverse of the core
+  for (int task = tid; task < 4 * z; task += NT) {
+    int blk = task / z, r = task - blk * z;
+    uint32_t acc = 0;
+    for (int t = 0; t < c.n_core_terms; t++) {
+      uint32_t ct = c.core_term[t];
+      if ((int)(ct >> 20) != blk) continue;
+      int src = (int)((ct >> 16) & 15u);
+      int cc = r + (int)(ct & 0xffffu);
+      cc -= (cc >= z) ? z : 0;
+      acc ^= syn[src * z + cc];
+    }
+    cw[c.k + task] = (uint8_t)acc;
+  }
+  __syncthreads();
+  // extension parity: row L >= 4 closes on its own parity bit k + L z + r
+  for (int task = 4 * z + tid; task < c.rows_n * z; task += NT) {
+    int L = task / z, r = task - L * z;
+    uint32_t acc = 0;
+    int own = c.k + task;
+    for (int t = c.layer_start[L]; t < c.layer_start[L + 1]; t++) {
+      int col = (int)(c.entry[t] >> 16) * z;
+      int cc = r + (int)(c.entry[t] & 0xffffu);
+      cc -= (cc >= z) ? z : 0;
+      col += cc;
+      if (col != own) acc ^= cw[col];
+    }
+    cw[own] = (uint8_t)acc;
+  }
+  __syncthreads();
+  // ---- labels, MSB first (bits_to_index, com-math bits.rs:68-70)
+  for (int s = tid; s < n_sym; s += NT) {
+    int idx = 0;
+    for (int b = 0; b < a.mbits; b++) {
+      int t = s * a.mbits + b;
+      int bit = t < c.e ? cw[c.map_is_offset ? 2 * z + t : c.map[t]] : pad[t - c.e];
+      idx = (idx << 1) | bit;
+    }
+    lab[s] = (uint8_t)idx;
+  }
+  __syncthreads();
+  // ---- measured power, summed in symbol order (com-math lib.rs:146-148)
+  if (tid == 0) {
+    double e = 0.0;
+    for (int s = 0; s < n_sym; s++) {
+      double re = pts[2 * lab[s]], im = pts[2 * lab[s] + 1];
+      e = __dadd_rn(e, __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
+    }
+    double p = __ddiv_rn(__dadd_rn(0.0, e), (double)n_sym);
+    s_sigma2 = __ddiv_rn(p, a.b_ebn0);
+  }
+  __syncthreads();
+  const double sigma2 = s_sigma2;
+  // ---- noise and demapping, symbol chunk [tid * spc, (tid + 1) * spc)
+  int s0 = tid * a.syms_per_chunk, s1 = min(s0 + a.syms_per_chunk, n_sym);
+  if (s0 >= s1) return;
+  cbd::Xoshiro r = cbd::stream(a.seed, a.name_hash, a.cond, fidx);
+  cbd::xoshiro_jump(r, a.jumps + 4 * (NT + tid));
+  T* out = a.llr_out + (size_t)frame * c.e;
+  if (sizeof(T) == 8) {
+    const double sd = __dsqrt_rn(sigma2);
+    const double uniform = -a.log_m;
+    for (int s = s0; s < s1; s++) {
+      double u1 = (double)(cbd::xoshiro_next(r) >> 11) * (1.0 / 9007199254740992.0);
+      double u2 = (double)(cbd::xoshiro_next(r) >> 11) * (1.0 / 9007199254740992.0);
+      double l = crm::cr_log(__dsub_rn(1.0, u1));
+      double rad = __dmul_rn(__dsqrt_rn(__dmul_rn(-2.0, l)), 0.70710678118654752440);
+      double sn, cs;
+      crm::cr_sincos(__dmul_rn(6.283185307179586, u2), &sn, &cs);
+      double nre = __dmul_rn(rad, cs), nim = __dmul_rn(rad, sn);
+      int li = lab[s];
+      double yre = __dadd_rn(pts[2 * li], __dmul_rn(nre, sd));
+      double yim = __dadd_rn(pts[2 * li + 1], __dmul_rn(nim, sd));
+      for (int o = 0; o < a.mbits; o++) {
+        int t = s * a.mbits + o;
+        if (t >= c.e) break;
+        int shift = a.mbits - 1 - o;
+        double m0 = -INFINITY, m1 = -INFINITY;
+        for (int i = 0; i < a.m; i++) {
+          double dr = __dsub_rn(yre, pts[2 * i]), di = __dsub_rn(yim, pts[2 * i + 1]);
+          double ns = __dadd_rn(__dmul_rn(dr, dr), __dmul_rn(di, di));
+          double met = __dadd_rn(__ddiv_rn(-ns, sigma2), uniform);
+          if ((i >> shift) & 1) m1 = fmax(m1, met);
+          else m0 = fmax(m0, met);
+        }
+        out[t] = (T)__dsub_rn(m0, m1);
+      }
+    }
+  } else {
+    const float sd = (float)__dsqrt_rn(sigma2);
+    const float inv_s2 = (float)(1.0 / sigma2);
+    const int h = a.mbits >> 1, side = 1 << h;
+    // the PAM levels of each dimension, ascending, with their Gray label parts:
+    // real level q is point gray(q), imaginary level q is point gray(side - 1 - q) * side
+    float lev_re[16], lev_im[16];
+    for (int q = 0; q < side; q++) {
+      lev_re[q] = (float)pts[2 * gray(q)];
+      lev_im[q] = (float)pts[2 * (gray(side - 1 - q) * side) + 1];
+    }
+    for (int s = s0; s < s1; s++) {
+      uint64_t x1 = cbd::xoshiro_next(r) >> 11, x2 = cbd::xoshiro_next(r) >> 11;
+      // 1 - u1 = (2^53 - x1) 2^-53 exactly, then rounded once to f32
+      float one_minus_u1 = __ull2float_rn((1ull << 53) - x1) * 1.1102230246251565e-16f;
+      float u2 = __ull2float_rn(x2 >> 29) * 5.9604644775390625e-08f;  // top 24 bits of u2
+      float rad = sqrtf(-2.0f * logf(one_minus_u1)) * 0.70710678f;
+      float sn, cs;
+      sincospif(2.0f * u2, &sn, &cs);
+      int li = lab[s];
+      float yre = (float)pts[2 * li] + rad * cs * sd;
+      float yim = (float)pts[2 * li + 1] + rad * sn * sd;
+      // label = gray(row) * side + gray(col): the first h bits come from the
+      // imaginary part, the last h from the real part
+      for (int o = 0; o < a.mbits; o++) {
+        int t = s * a.mbits + o;
+        if (t >= c.e) break;
+        bool upper = o < h;
+        int bitpos = upper ? (h - 1 - o) : (a.mbits - 1 - o);
+        float y = upper ? yim : yre;
+        float m0 = -INFINITY, m1 = -INFINITY;
+        for (int q = 0; q < side; q++) {
+          int lbl = upper ? gray(side - 1 - q) : gray(q);
+          float dd = y - (upper ? lev_im[q] : lev_re[q]);
+          float met = -(dd * dd) * inv_s2;
+          if ((lbl >> bitpos) & 1) m1 = fmaxf(m1, met);
+          else m0 = fmaxf(m0, met);
+        }
+        out[t] = (T)(m0 - m1);
+      }
+    }
+  }
+}
+
+}  // namespace
+
+size_t gen_smem_bytes(const cbd::DevCode& c, int m, int mbits, int n_pad) {
+  int n_sym = (c.e + n_pad) / mbits;
+  return (size_t)2 * m * sizeof(double) + 4 * c.z + c.n_full + n_sym + 16;
+}
+
+template <typename T>
+cudaError_t launch_gen(const GenArgs<T>& a, cudaStream_t stream) {
+  size_t smem = gen_smem_bytes(a.code, a.m, a.mbits, a.n_pad);
+  void* k = (void*)gen_kernel<T>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {(void*)&a};
+  return cudaLaunchKernel(k, dim3((unsigned)a.n_frames), dim3(NT), args, smem, stream);
+}
+
+template cudaError_t launch_gen<double>(const GenArgs<double>&, cudaStream_t);
+template cudaError_t launch_gen<float>(const GenArgs<float>&, cudaStream_t);
+
+}  // namespace cbk

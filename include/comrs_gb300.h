@@ -1,0 +1,144 @@
+/* comrs_gb300.h -- C ABI of the GB300 BICM-LDPC Monte Carlo trial.
+ *
+ * The drop-in boundary of com-rs's BICM-LDPC hot path (5G NR LDPC encode, Gray QAM,
+ * AWGN, max-log demap, layered min-sum decode, error counts) on one GPU.  Every call
+ * returns a status; host buffers are caller-owned; device buffers belong to the code
+ * object.  Calls on one code object are serialised by an internal mutex.
+ *
+ * Reference interfaces replaced (paths inside the com-rs project):
+ *   cb_code_create        NrLdpc::with_options + LdpcDecoder settings
+ *                         (crates/com-fec/src/nr/ldpc.rs:101-162,
+ *                          crates/com-fec/src/ldpc.rs:165-172, :113-123)
+ *   cb_encode             BlockCode::encode_block of NrLdpc (nr/ldpc.rs:209-214)
+ *   cb_decode             BlockCode::decode_block / SoftDecode::app_into of NrLdpc
+ *                         (nr/ldpc.rs:216-240), batched
+ *   cb_run_frames         the body of Scenario::trial for a BICM-LDPC link, frame f
+ *                         drawing from stream(seed, name, condition, f)
+ *                         (crates/com-sim/src/runner.rs:435-447,
+ *                          crates/com-sim/src/scenario.rs:201-219)
+ *   status codes          com_core::Error::{Config, Shape, Numerical, Condition, Io}
+ *                         (crates/com-core/src/error.rs:25-40)
+ */
+#ifndef COMRS_GB300_H
+#define COMRS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  CB_OK = 0,
+  CB_ERR_CONFIG = -1,    /* invalid settings (Error::Config) */
+  CB_ERR_SHAPE = -2,     /* wrong buffer sizes (Error::Shape) */
+  CB_ERR_NUMERICAL = -3, /* Error::Numerical */
+  CB_ERR_CONDITION = -4, /* Error::Condition */
+  CB_ERR_IO = -5,        /* Error::Io */
+  CB_ERR_CUDA = -6,      /* a CUDA call failed */
+  CB_ERR_TIMEOUT = -7    /* a bounded device wait ran out */
+} cb_status;
+
+typedef enum { CB_RULE_SUM_PRODUCT = 0, CB_RULE_NMS = 1, CB_RULE_OMS = 2 } cb_rule;
+typedef enum { CB_F64 = 0, CB_F32 = 1 } cb_precision;
+
+/* Code and decoder settings.  Keyword surface of the reference's Python NrLdpc
+ * (bindings/com-py/src/fec/nr.rs:52-83). */
+typedef struct {
+  int32_t k_info;         /* K': information bits per code block */
+  int32_t e;              /* E: transmitted bits (rate matching output) */
+  int32_t base_graph;     /* 0: the TS 38.212 rule (nr/ldpc.rs:78-81); 1 or 2 forced */
+  int32_t lifting_size;   /* 0: smallest Z with kb Z >= K' (nr/ldpc.rs:117-123); else forced */
+  int32_t rv;             /* redundancy version 0..3 */
+  int32_t qm;             /* bit interleaver rows (1: none) */
+  int32_t rule;           /* cb_rule */
+  double alpha;           /* NMS scale or OMS offset */
+  int32_t layered;        /* 1: layered schedule (only layered is built on the GPU) */
+  int32_t max_iterations; /* >= 0 */
+  int32_t precision;      /* cb_precision: arithmetic of LLRs and messages */
+  int32_t device;         /* CUDA device ordinal */
+} cb_code_desc;
+
+/* Per-frame record of cb_run_frames, in frame order (8 bytes). */
+typedef struct {
+  uint32_t bit_errors; /* errors among the K' information bits */
+  uint8_t frame_error; /* bit_errors > 0 */
+  uint8_t iterations;  /* decoder iterations (0: the channel word was a codeword) */
+  uint16_t reserved;
+} cb_frame_result;
+
+typedef struct cb_code cb_code;
+
+/* Library version string. */
+const char* cb_version(void);
+
+/* Build a code on a device.  *out is NULL on error; cb_last_error(NULL) names it. */
+cb_status cb_code_create(const cb_code_desc* desc, cb_code** out);
+void cb_code_destroy(cb_code* code);
+
+/* The message of the last error of `code` (or of the calling thread when NULL). */
+const char* cb_last_error(const cb_code* code);
+
+/* info[0..16): base graph, Z, K', E, K (systematic columns), n_full, lifted rows,
+ * edges, iLS, max row degree, rv, qm, core-inverse terms, 1 if the rate matching is
+ * the plain offset 2Z + t, 0, 0. */
+cb_status cb_code_info(const cb_code* code, int64_t info[16]);
+
+/* The construction tables: `entries` = n_entries records (base row, base column,
+ * shift mod Z) in layer order; `bit_map` = the E rate-matching positions.  Either
+ * pointer may be NULL.  Sizes from cb_code_info. */
+cb_status cb_code_tables(const cb_code* code, int32_t* entries, int32_t* bit_map);
+
+/* Encode n_frames blocks: info = n_frames x K' bytes (0/1), out = n_frames x E bytes. */
+cb_status cb_encode(cb_code* code, const uint8_t* info, int64_t n_frames, uint8_t* out);
+
+/* Decode n_frames blocks of E channel LLRs (double for CB_F64, float for CB_F32),
+ * host buffers.  bits: n_frames x ceil(K'/8) bytes, packed LSB first (optional);
+ * app: n_frames x K' a posteriori LLRs of the information bits (optional);
+ * iterations: n_frames int32 (optional). */
+cb_status cb_decode(cb_code* code, const void* llr, int64_t n_frames, uint8_t* bits, void* app,
+                    int32_t* iterations);
+
+/* cb_decode on device buffers and a caller stream (cudaStream_t, NULL = default):
+ * bits: n_frames x ceil(K'/32) uint32 words, packed LSB first. */
+cb_status cb_decode_device(cb_code* code, const void* llr_dev, int64_t n_frames, uint32_t* bits_dev,
+                           void* app_dev, int32_t* iterations_dev, void* stream);
+
+/* Monte Carlo frames [first_frame, first_frame + n_frames) of one condition: frame f
+ * draws its K' bits, padding bits and noise from stream(seed, name, condition, f), with
+ * name_hash = FNV-1a 64 of the scenario name (crates/com-core/src/rng.rs:58-65).
+ * modulation_order: 4, 16, 64 or 256 (Gray square QAM, unit energy).  Results in
+ * frame order into `out` (host, n_frames records). */
+cb_status cb_run_frames(cb_code* code, int32_t modulation_order, uint64_t seed, uint64_t name_hash,
+                        uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,
+                        cb_frame_result* out);
+
+/* The E channel LLRs and the K' information bits of frames [first_frame, +n_frames)
+ * as cb_run_frames draws them (llr: n_frames x E, double or float by precision;
+ * info: n_frames x K' bytes).  For checks and for LLR dumps. */
+cb_status cb_generate_frames(cb_code* code, int32_t modulation_order, uint64_t seed, uint64_t name_hash,
+                             uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,
+                             void* llr, uint8_t* info);
+
+/* cb_run_frames on a caller stream (cudaStream_t, NULL = default) with the per-frame
+ * records in device memory (results_dev: n_frames records).  The LLR scratch belongs to
+ * the code object.  Asynchronous: the caller synchronises its stream. */
+cb_status cb_run_frames_device(cb_code* code, int32_t modulation_order, uint64_t seed, uint64_t name_hash,
+                               uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,
+                               cb_frame_result* results_dev, void* stream);
+
+/* cb_generate_frames on a caller stream into device buffers: llr_dev n_frames x E
+ * (double or float), info_dev n_frames x ceil(K'/32) uint32 words, LSB first. */
+cb_status cb_generate_frames_device(cb_code* code, int32_t modulation_order, uint64_t seed, uint64_t name_hash,
+                                    uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,
+                                    void* llr_dev, uint32_t* info_dev, void* stream);
+
+/* The state of the xoshiro256** generator after `steps` draws from `state` (jump-ahead
+ * by a polynomial; Rng::state / Rng::from_state, crates/com-core/src/rng.rs:83-96). */
+cb_status cb_xoshiro_jump(const uint64_t state[4], uint64_t steps, uint64_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COMRS_GB300_H */

@@ -1,0 +1,47 @@
+"""Re-create the golden fixtures of this directory from the reference's own test data.
+
+Run in a checkout where the com-rs sources are available (they are not needed to run the
+tests):  ``python tests/golden/make_golden.py <com-rs root>``
+
+Outputs (committed):
+  * ``sionna_nr_ldpc.npz`` -- the 28 NR-LDPC (K', E) encodings of the reference's
+    fixture ``tests/oracle/sionna_vectors.npz`` (keys ``ldpc.k{K}_n{E}.{u,c}``,
+    Apache-2.0, provenance in ``tests/oracle/sionna_vectors.json`` of com-rs), stored
+    with np.packbits along the last axis (shape kept in ``<key>.shape``);
+  * ``aff3ct_peg_n576_k288_layered_nms075_i20.json`` -- the AFF3CT FER/BER curve of the
+    layered normalised min-sum (alpha 0.75, 20 iterations) on the PEG(576, 288) matrix
+    (``validation/aff3ct/`` of com-rs), and ``peg_n576_k288.alist``, its matrix.
+"""
+
+import json
+import os
+import shutil
+import sys
+
+import numpy as np
+
+
+def main():
+    root = sys.argv[1] if len(sys.argv) > 1 else "."
+    here = os.path.dirname(os.path.abspath(__file__))
+    src = np.load(os.path.join(root, "tests/oracle/sionna_vectors.npz"))
+    out = {}
+    for k in sorted(src.files):
+        if not k.startswith("ldpc."):
+            continue
+        a = np.asarray(src[k], dtype=np.uint8)
+        out[k] = np.packbits(a, axis=-1)
+        out[k + ".shape"] = np.array(a.shape, dtype=np.int64)
+    np.savez_compressed(os.path.join(here, "sionna_nr_ldpc.npz"), **out)
+    prov = json.load(open(os.path.join(root, "tests/oracle/sionna_vectors.json")))
+    json.dump({"source": "com-rs tests/oracle/sionna_vectors.npz", "upstream_commit": prov.get("commit"),
+               "keys": sorted(k for k in out if not k.endswith(".shape"))},
+              open(os.path.join(here, "sionna_nr_ldpc.json"), "w"), indent=1)
+    aff = "validation/aff3ct/ldpc_peg_n576_k288_layered_nms075_i20.json"
+    shutil.copy(os.path.join(root, aff), os.path.join(here, os.path.basename(aff)))
+    shutil.copy(os.path.join(root, "validation/aff3ct/matrices/peg_n576_k288.alist"),
+                os.path.join(here, "peg_n576_k288.alist"))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,147 @@
+"""GPU decoder parity: the CUDA layered min-sum against the oracle on LLR dumps.
+
+f64: hard decisions, iteration counts and a posteriori LLRs bit-identical to the oracle's
+restatement of LdpcCode::propagate.  f32: bit-identical to the same algorithm in f32,
+and within 1e-5 relative of the f64 decoder wherever the two agree on the decisions.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import sionna_vectors
+
+pytestmark = pytest.mark.gpu
+
+SEED = 7
+
+CODES = [
+    dict(k=520, e=1040, bg=2, z=52, m=4, ebn0=(0.5, 1.5, 2.5)),      # benchmark config 1
+    dict(k=100, e=300, m=4, ebn0=(1.0, 3.0)),                         # fillers (K' < K)
+    dict(k=500, e=1200, rv=2, qm=4, m=16, ebn0=(2.0, 4.0)),
+    dict(k=60, e=1000, rv=1, qm=2, m=4, ebn0=(-2.0,)),               # repeated bits
+    dict(k=1056, e=3168, bg=1, z=48, m=16, ebn0=(1.5, 3.0)),
+    dict(k=8448, e=25344, bg=1, z=384, m=16, ebn0=(2.5, 3.0)),       # benchmark config 2
+]
+
+
+def dump(O, spec, n, ebn0, cond=0):
+    code = O.Code(spec["k"], spec["e"], bg=spec.get("bg", 0), z=spec.get("z", 0), rv=spec.get("rv", 0),
+                  qm=spec.get("qm", 1))
+    code.set_decoder(O.RULE_NMS, 0.75, True, 20)
+    llr = np.zeros((n, spec["e"]))
+    h = O.fnv1a64("dump")
+    for f in range(n):
+        _, llr[f], _ = code.trial(spec["m"], SEED, h, cond, f, ebn0)
+    return code, llr
+
+
+def gpu_code(cb, spec, precision, rule="normalized_min_sum", alpha=0.75, it=20):
+    return cb.NrLdpc(spec["k"], spec["e"], base_graph=spec.get("bg"), lifting_size=spec.get("z"),
+                     rv=spec.get("rv", 0), qm=spec.get("qm", 1), precision=precision, rule=rule, alpha=alpha,
+                     max_iterations=it)
+
+
+@pytest.mark.parametrize("spec", CODES, ids=lambda s: f"k{s['k']}_e{s['e']}")
+def test_f64_decode_is_bit_exact(cb, O, spec):
+    n = 6 if spec["k"] > 4000 else 24
+    g = gpu_code(cb, spec, "f64")
+    for eb in spec["ebn0"]:
+        ref, llr = dump(O, spec, n, eb)
+        bits, app, it = g.decode_full(llr)
+        for f in range(n):
+            rb, rit, rapp, _ = ref.decode(llr[f], "f64", want_app=True)
+            assert np.array_equal(bits[f], rb), (eb, f)
+            assert it[f] == rit, (eb, f, it[f], rit)
+            assert np.array_equal(app[f].view(np.uint64), rapp.view(np.uint64)), (eb, f)
+
+
+@pytest.mark.parametrize("spec", CODES, ids=lambda s: f"k{s['k']}_e{s['e']}")
+def test_f32_decode_is_bit_exact_to_the_f32_oracle(cb, O, spec):
+    n = 6 if spec["k"] > 4000 else 24
+    g = gpu_code(cb, spec, "f32")
+    for eb in spec["ebn0"]:
+        ref, llr = dump(O, spec, n, eb)
+        l32 = llr.astype(np.float32)
+        bits, app, it = g.decode_full(l32)
+        for f in range(n):
+            rb, rit, rapp, _ = ref.decode(l32[f], "f32", want_app=True)
+            assert np.array_equal(bits[f], rb) and it[f] == rit
+            assert np.array_equal(app[f].view(np.uint32), rapp.view(np.uint32))
+
+
+def test_f32_is_within_1e5_of_the_f64_decoder(cb, O):
+    # the f32 messages against com-fec's f64 decoder on the same (f64-dumped) LLRs
+    spec = CODES[0]
+    g32, g64 = gpu_code(cb, spec, "f32"), gpu_code(cb, spec, "f64")
+    _, llr = dump(O, spec, 64, 2.0)
+    b32, a32, i32 = g32.decode_full(llr.astype(np.float32))
+    b64, a64, i64 = g64.decode_full(llr)
+    same = np.all(b32 == b64, axis=1) & (i32 == i64)
+    assert same.mean() >= 0.95
+    rel = np.abs(a32[same].astype(np.float64) - a64[same]) / np.maximum(np.abs(a64[same]), 1.0)
+    assert rel.max() <= 1e-5, rel.max()
+
+
+@pytest.mark.parametrize("rule,alpha", [("offset_min_sum", 0.15), ("min_sum", 1.0), ("normalized_min_sum", 0.8)])
+def test_other_min_sum_rules(cb, O, rule, alpha):
+    spec = CODES[0]
+    ref, llr = dump(O, spec, 16, 1.5)
+    ref.set_decoder(O.RULE_OMS if rule == "offset_min_sum" else O.RULE_NMS, alpha, True, 20)
+    g = gpu_code(cb, spec, "f64", rule=rule, alpha=alpha)
+    bits, app, it = g.decode_full(llr)
+    for f in range(16):
+        rb, rit, rapp, _ = ref.decode(llr[f], "f64", want_app=True)
+        assert np.array_equal(bits[f], rb) and it[f] == rit
+        assert np.array_equal(app[f].view(np.uint64), rapp.view(np.uint64))
+
+
+def test_sionna_vectors_decode_on_the_gpu(cb):
+    # tests/test_sionna_vectors.py:104-115 of com-rs: decode(4 - 8c) == u for K' <= 1024
+    vec, pairs = sionna_vectors()
+    for k, n in pairs:
+        if k > 1024:
+            continue
+        u, c = vec[f"ldpc.k{k}_n{n}.u"], vec[f"ldpc.k{k}_n{n}.c"]
+        for precision in ("f64", "f32"):
+            g = cb.NrLdpc(k, n, max_iterations=50, precision=precision)
+            assert np.array_equal(g.decode(4.0 - 8.0 * c.astype(np.float64)), u), (k, n, precision)
+
+
+def test_edge_cases(cb, O):
+    spec = CODES[0]
+    g = gpu_code(cb, spec, "f64")
+    # no frames
+    assert g.decode(np.zeros((0, 1040))).shape == (0, 520)
+    # all-zero LLRs: the all-zero word is a codeword, zero iterations
+    bits, app, it = g.decode_full(np.zeros(1040))
+    assert it == 0 and not bits.any()
+    # negative zeros, huge magnitudes and a codeword: as the oracle
+    ref = O.Code(520, 1040, bg=2, z=52).set_decoder(O.RULE_NMS, 0.75, True, 20)
+    rng = np.random.default_rng(3)
+    info = rng.integers(0, 2, 520, dtype=np.uint8)
+    cw = ref.encode(info)
+    for llr in (np.where(cw == 1, -0.0, 0.0), 1e300 * (1 - 2.0 * cw), (1 - 2.0 * cw) * 3.0,
+                np.where(rng.random(1040) < 0.3, -0.0, (1 - 2.0 * cw) * rng.random(1040))):
+        b, a, i = g.decode_full(llr)
+        rb, ri, ra, _ = ref.decode(llr, "f64", want_app=True)
+        assert np.array_equal(b, rb) and i == ri
+        assert np.array_equal(a.view(np.uint64), ra.view(np.uint64))
+    # max_iterations = 0 returns the channel decisions
+    g0 = gpu_code(cb, spec, "f64", it=0)
+    ref.set_decoder(O.RULE_NMS, 0.75, True, 0)
+    _, llr = dump(O, spec, 4, 0.0)
+    b, a, i = g0.decode_full(llr)
+    for f in range(4):
+        rb, ri, _, _ = ref.decode(llr[f], "f64")
+        assert np.array_equal(b[f], rb) and i[f] == ri == 0
+
+
+def test_many_frames_in_one_launch(cb, O):
+    # more frames than resident CTAs: the persistent grid's work stealing covers them all
+    spec = CODES[0]
+    ref, llr = dump(O, spec, 40, 1.0)
+    big = np.tile(llr, (60, 1))
+    g = gpu_code(cb, spec, "f64")
+    bits, app, it = g.decode_full(big)
+    bits1, app1, it1 = g.decode_full(llr)
+    assert np.array_equal(bits, np.tile(bits1, (60, 1))) and np.array_equal(it, np.tile(it1, 60))

@@ -1,0 +1,110 @@
+"""GPU Monte Carlo trial parity: frames regenerated on the device from their streams.
+
+f64: the E channel LLRs and the K' info bits of every frame are bit-identical to the
+oracle's (correctly-rounded noise mode), and so are the per-frame bit errors, frame
+errors and iteration counts.  f32: same bits, noise in f32, statistically equal FER.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NAME = "bicm_ldpc"
+
+CODES = [
+    dict(k=520, e=1040, bg=2, z=52, m=4),           # benchmark config 1
+    dict(k=100, e=302, m=16),                       # 2 padding bits, fillers
+    dict(k=500, e=1200, rv=2, qm=4, m=64),
+    dict(k=1000, e=1504, m=256),
+    dict(k=8448, e=25344, bg=1, z=384, m=16),       # benchmark config 2
+    dict(k=8448, e=16896, bg=1, z=384, m=64),       # benchmark config 5
+]
+
+
+def codes(cb, O, spec, precision="f64"):
+    g = cb.NrLdpc(spec["k"], spec["e"], base_graph=spec.get("bg"), lifting_size=spec.get("z"),
+                  rv=spec.get("rv", 0), qm=spec.get("qm", 1), precision=precision)
+    r = O.Code(spec["k"], spec["e"], bg=spec.get("bg", 0), z=spec.get("z", 0), rv=spec.get("rv", 0),
+               qm=spec.get("qm", 1)).set_decoder(O.RULE_NMS, 0.75, True, 20)
+    return g, r
+
+
+@pytest.mark.parametrize("spec", CODES, ids=lambda s: f"k{s['k']}_e{s['e']}_m{s['m']}")
+def test_f64_frames_are_the_oracle_frames(cb, O, spec):
+    g, r = codes(cb, O, spec)
+    n = 3 if spec["k"] > 4000 else 12
+    for cond, eb in enumerate((0.5, 2.0)):
+        llr, info = g.generate_frames(7, NAME, cond, 5, n, eb, spec["m"])
+        for f in range(n):
+            rinfo, rllr, _ = r.trial(spec["m"], 7, O.fnv1a64(NAME), cond, 5 + f, eb, 0, O.NOISE_CR)
+            assert np.array_equal(info[f], rinfo), (cond, f)
+            assert np.array_equal(llr[f].view(np.uint64), rllr.view(np.uint64)), (cond, f)
+
+
+@pytest.mark.parametrize("eb", [0.0, 1.0, 2.0, 3.0])
+def test_f64_counts_equal_the_oracle(cb, O, eb):
+    spec = CODES[0]
+    g, r = codes(cb, O, spec)
+    got = g.run_frames(7, NAME, 3, 0, 400, eb, 4)
+    want = r.run_frames(4, 7, O.fnv1a64(NAME), 3, 0, 400, eb, 0, O.NOISE_CR, 0)
+    for key in ("bit_errors", "frame_error", "iterations"):
+        assert np.array_equal(got[key], want[key]), key
+
+
+def test_f32_frames_draw_the_same_bits_and_close_llrs(cb, O):
+    spec = CODES[4]
+    g32, _ = codes(cb, O, spec, "f32")
+    g64, _ = codes(cb, O, spec, "f64")
+    l32, i32 = g32.generate_frames(7, NAME, 0, 0, 4, 1.0, 16)
+    l64, i64 = g64.generate_frames(7, NAME, 0, 0, 4, 1.0, 16)
+    assert np.array_equal(i32, i64)
+    err = np.abs(l32.astype(np.float64) - l64) / np.maximum(np.abs(l64), 1.0)
+    assert np.median(err) < 1e-5 and err.max() < 1e-3
+    assert np.mean(np.sign(l32) == np.sign(l64)) > 0.9999
+
+
+def test_f32_fer_is_statistically_the_f64_fer(cb, O):
+    from conftest import load_package
+
+    ErrorRate = load_package().campaign.ErrorRate
+    spec = CODES[0]
+    g32, _ = codes(cb, O, spec, "f32")
+    g64, _ = codes(cb, O, spec, "f64")
+    for eb in (1.0, 1.5):
+        a = g32.run_frames(7, NAME, 0, 0, 20000, eb, 4)
+        b = g64.run_frames(7, NAME, 0, 0, 20000, eb, 4)
+        ra = ErrorRate(int(a["frame_error"].sum()), len(a))
+        rb = ErrorRate(int(b["frame_error"].sum()), len(b))
+        (a0, a1), (b0, b1) = ra.wilson(0.99), rb.wilson(0.99)
+        assert not (a1 < b0 or b1 < a0), (eb, ra.rate(), rb.rate())
+
+
+def test_frames_do_not_depend_on_the_batching(cb, O):
+    spec = CODES[0]
+    g, _ = codes(cb, O, spec, "f32")
+    whole = g.run_frames(7, NAME, 1, 100, 3000, 1.0, 4)
+    parts = np.concatenate([g.run_frames(7, NAME, 1, 100, 1234, 1.0, 4),
+                            g.run_frames(7, NAME, 1, 1334, 1766, 1.0, 4)])
+    assert np.array_equal(whole, parts)
+    assert np.array_equal(whole, g.run_frames(7, NAME, 1, 100, 3000, 1.0, 4))
+
+
+def test_large_code_high_snr_decodes_everything(cb, O):
+    spec = CODES[4]
+    g, _ = codes(cb, O, spec, "f32")
+    r = g.run_frames(7, NAME, 0, 0, 512, 4.0, 16)
+    assert r["frame_error"].sum() == 0 and r["iterations"].max() <= 12
+
+
+def test_campaign_counts_match_the_frames(cb, O):
+    spec = CODES[0]
+    g, r = codes(cb, O, spec)
+    grid = cb.Grid().axis("ebn0_db", [0.0, 2.0])
+    res = cb.run(g, grid, cb.Stop.min_errors("fer", 50).or_(cb.Stop.max_trials(700)), seed=7, name=NAME,
+                 batch=256, modulation=4)
+    assert res[0].trials == 256 and res[1].trials == 700  # the bound is met exactly
+    for c, eb in enumerate((0.0, 2.0)):
+        want = r.run_frames(4, 7, O.fnv1a64(NAME), c, 0, res[c].trials, eb, 0, O.NOISE_CR, 0)
+        assert res[c].record["fer"].errors == int(want["frame_error"].sum())
+        assert res[c].record["ber"].errors == int(want["bit_errors"].sum())
