@@ -126,10 +126,10 @@ cudaError_t grow(P*& ptr, size_t& cap, size_t bytes) {
 
 size_t elem_size(const cb_code* c) { return c->precision == CB_F64 ? sizeof(double) : sizeof(float); }
 
-// frames per launch chunk: bounded so the scratch stays a few hundred MB
+// frames per launch chunk of the host-buffer calls: the LLR scratch stays within 2 GB
 int64_t chunk_frames(const cb_code* c) {
   size_t per = (size_t)c->host.e * elem_size(c) + 64;
-  int64_t n = (int64_t)((size_t)512 << 20) / (int64_t)per;
+  int64_t n = (int64_t)((size_t)2048 << 20) / (int64_t)per;
   return std::max<int64_t>(1, std::min<int64_t>(n, 65536));
 }
 
@@ -380,6 +380,14 @@ cb_status cb_code_create(const cb_code_desc* d, cb_code** out) {
   if (!cbh::build_nr_code(spec, c->host, err)) {
     delete c;
     return fail(nullptr, CB_ERR_CONFIG, err);
+  }
+  // the decoder is compiled for the row degrees of the NR base graphs
+  for (int L = 0; L < c->host.rows_n; L++) {
+    int deg = c->host.layer_start[L + 1] - c->host.layer_start[L];
+    if (!((deg >= 3 && deg <= 10) || deg == 19)) {
+      delete c;
+      return fail(nullptr, CB_ERR_CONFIG, "a base-graph row degree outside 3..10 and 19");
+    }
   }
   c->device = d->device;
   c->precision = d->precision;

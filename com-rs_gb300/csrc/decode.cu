@@ -82,7 +82,76 @@ __device__ __forceinline__ bool some_check_fails(const cbd::DevCode& c, const T*
   return __syncthreads_or(bad) != 0;
 }
 
-template <typename T, int MAXD>
+// One lifted row of a layer: thread r, degree D known at compile time.
+// old state (a1, a2, mt) -> new state (n1, n2, nm); post updated in place.
+template <typename T, int D>
+__device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t* __restrict__ ent, int r, int z,
+                                           T a1, T a2, uint32_t mt, int rule, T alpha, T& n1, T& n2,
+                                           uint32_t& nm) {
+  int off[D];
+  T x[D];
+  const int old_i1 = (int)(mt & 31u);
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    const uint32_t en = ent[e];
+    // (r + shift) mod Z with one unsigned min: r + shift < 2Z
+    unsigned c = (unsigned)r + (en & 0xffffu);
+    unsigned cm = c - (unsigned)z;
+    off[e] = (int)(en >> 16) * z + (int)min(c, cm);
+    T mag = (e == old_i1) ? a2 : a1;
+    T old = ((mt >> (8 + e)) & 1u) ? -mag : mag;
+    x[e] = sub_rn(post[off[e]], old);
+  }
+  // check_message, min-sum branch (ldpc.rs:468-491): sign product with `l < 0`, strict
+  // `<` for the minimum and its index, min(m2, a) for the second (equal for non-NaN,
+  // and a NaN is skipped by both)
+  uint32_t par = (uint32_t)(x[0] < (T)0);
+  T m1 = fmin(fabs(x[0]), infinity<T>()), m2 = infinity<T>();
+  int i1 = 0;
+#pragma unroll
+  for (int e = 1; e < D; e++) {
+    par ^= (uint32_t)(x[e] < (T)0);
+    T av = fabs(x[e]);
+    bool lt = av < m1;
+    m2 = lt ? m1 : fmin(m2, av);
+    m1 = lt ? av : m1;
+    i1 = lt ? e : i1;
+  }
+  if (rule == cbd::RULE_NMS) {
+    n1 = mul_rn(alpha, m1);
+    n2 = mul_rn(alpha, m2);
+  } else {
+    n1 = fmax(sub_rn(m1, alpha), (T)0);
+    n2 = fmax(sub_rn(m2, alpha), (T)0);
+  }
+  nm = (uint32_t)i1;
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    uint32_t ng = par ^ (uint32_t)(x[e] < (T)0);
+    T mag = (e == i1) ? n2 : n1;
+    T o = ng ? -mag : mag;
+    post[off[e]] = add_rn(x[e], o);
+    nm |= ng << (8 + e);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent, int r, int z, T a1, T a2,
+                                             uint32_t mt, int rule, T alpha, T& n1, T& n2, uint32_t& nm) {
+  switch (d) {
+    case 3: row_update<T, 3>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 4: row_update<T, 4>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 5: row_update<T, 5>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 6: row_update<T, 6>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 7: row_update<T, 7>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 8: row_update<T, 8>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 9: row_update<T, 9>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 10: row_update<T, 10>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    default: row_update<T, 19>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+  }
+}
+
+template <typename T>
 __global__ void __launch_bounds__(384) layered_kernel(const __grid_constant__ DecodeArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   T* post = reinterpret_cast<T*>(smem);
@@ -100,6 +169,7 @@ __global__ void __launch_bounds__(384) layered_kernel(const __grid_constant__ De
   const int rule = a.cfg.rule;
   const int max_it = a.cfg.max_iterations;
   const int wpf = (c.k_info + 31) >> 5;
+  const bool active = tid < z;
 
   for (;;) {
     if (tid == 0) {
@@ -136,71 +206,37 @@ __global__ void __launch_bounds__(384) layered_kernel(const __grid_constant__ De
     if (some_check_fails(c, post, tid)) {
       it = max_it;
       for (int iter = 1; iter <= max_it; iter++) {
+        // the state of a layer is prefetched one layer ahead
+        T a1 = (T)0, a2 = (T)0;
+        uint32_t mt = 0;
+        if (iter > 1 && active) {
+          a1 = A1[tid];
+          a2 = A2[tid];
+          mt = meta[tid];
+        }
         for (int L = 0; L < c.rows_n; L++) {
-          if (tid < z) {
+          T p1 = (T)0, p2 = (T)0;
+          uint32_t pm = 0;
+          if (iter > 1 && active && L + 1 < c.rows_n) {
+            const int nrow = (L + 1) * z + tid;
+            p1 = A1[nrow];
+            p2 = A2[nrow];
+            pm = meta[nrow];
+          }
+          if (active) {
             const int s0 = c.layer_start[L];
             const int d = c.layer_start[L + 1] - s0;
-            const int row = L * z + tid;
-            T a1 = (T)0, a2 = (T)0;
-            uint32_t mt = 0;
-            if (iter > 1) {
-              a1 = A1[row];
-              a2 = A2[row];
-              mt = meta[row];
-            }
-            T x[MAXD];
-            int col[MAXD];
-            const int old_i1 = (int)(mt & 31u);
-#pragma unroll
-            for (int e = 0; e < MAXD; e++) {
-              if (e < d) {
-                col[e] = lifted_col(c.entry[s0 + e], tid, z);
-                T mag = (e == old_i1) ? a2 : a1;
-                T old = ((mt >> (8 + e)) & 1u) ? -mag : mag;
-                x[e] = sub_rn(post[col[e]], old);
-              }
-            }
-            // check_message, min-sum branch (ldpc.rs:468-491)
-            uint32_t par = 0;
-            T m1 = infinity<T>(), m2 = infinity<T>();
-            int i1 = 0;
-#pragma unroll
-            for (int e = 0; e < MAXD; e++) {
-              if (e < d) {
-                par ^= (uint32_t)(x[e] < (T)0);
-                T av = fabs(x[e]);
-                if (av < m1) {
-                  m2 = m1;
-                  m1 = av;
-                  i1 = e;
-                } else if (av < m2) {
-                  m2 = av;
-                }
-              }
-            }
             T n1, n2;
-            if (rule == cbd::RULE_NMS) {
-              n1 = mul_rn(alpha, m1);
-              n2 = mul_rn(alpha, m2);
-            } else {
-              n1 = fmax(sub_rn(m1, alpha), (T)0);
-              n2 = fmax(sub_rn(m2, alpha), (T)0);
-            }
-            uint32_t nm = (uint32_t)i1;
-#pragma unroll
-            for (int e = 0; e < MAXD; e++) {
-              if (e < d) {
-                uint32_t ng = par ^ (uint32_t)(x[e] < (T)0);
-                T mag = (e == i1) ? n2 : n1;
-                T o = ng ? -mag : mag;
-                post[col[e]] = add_rn(x[e], o);
-                nm |= ng << (8 + e);
-              }
-            }
+            uint32_t nm;
+            row_dispatch<T>(d, post, c.entry + s0, tid, z, a1, a2, mt, rule, alpha, n1, n2, nm);
+            const int row = L * z + tid;
             A1[row] = n1;
             A2[row] = n2;
             meta[row] = nm;
           }
+          a1 = p1;
+          a2 = p2;
+          mt = pm;
           __syncthreads();
         }
         if (!some_check_fails(c, post, tid)) {
@@ -246,8 +282,8 @@ __global__ void __launch_bounds__(384) layered_kernel(const __grid_constant__ De
 
 template <typename T>
 void* kernel_for(int max_degree) {
-  if (max_degree <= 10) return (void*)layered_kernel<T, 10>;
-  return (void*)layered_kernel<T, 19>;
+  (void)max_degree;
+  return (void*)layered_kernel<T>;
 }
 
 int block_threads(int z) { return ((z + 31) / 32) * 32; }

@@ -54,6 +54,7 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
   uint8_t* lab = cw + c.n_full;
   uint8_t* pad = lab + n_sym;  // padding bits (< mbits)
   __shared__ double s_sigma2;
+  __shared__ unsigned int s_hist[256];
   const long long frame = (long long)blockIdx.x;
   if (frame >= a.n_frames) return;
   const uint64_t fidx = a.first_frame + (uint64_t)frame;
@@ -140,15 +141,32 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
     lab[s] = (uint8_t)idx;
   }
   __syncthreads();
-  // ---- measured power, summed in symbol order (com-math lib.rs:146-148)
-  if (tid == 0) {
-    double e = 0.0;
-    for (int s = 0; s < n_sym; s++) {
-      double re = pts[2 * lab[s]], im = pts[2 * lab[s] + 1];
-      e = __dadd_rn(e, __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
+  // ---- measured power (com-math lib.rs:146-148)
+  if (sizeof(T) == 8) {
+    // f64 frames: summed in symbol order, as the reference
+    if (tid == 0) {
+      double e = 0.0;
+      for (int s = 0; s < n_sym; s++) {
+        double re = pts[2 * lab[s]], im = pts[2 * lab[s] + 1];
+        e = __dadd_rn(e, __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
+      }
+      double p = __ddiv_rn(__dadd_rn(0.0, e), (double)n_sym);
+      s_sigma2 = __ddiv_rn(p, a.b_ebn0);
     }
-    double p = __ddiv_rn(__dadd_rn(0.0, e), (double)n_sym);
-    s_sigma2 = __ddiv_rn(p, a.b_ebn0);
+  } else {
+    // f32 frames: the label histogram, then the sum over the M labels
+    for (int i = tid; i < a.m; i += NT) s_hist[i] = 0;
+    __syncthreads();
+    for (int s = tid; s < n_sym; s += NT) atomicAdd(&s_hist[lab[s]], 1u);
+    __syncthreads();
+    if (tid == 0) {
+      float e = 0.0f;
+      for (int i = 0; i < a.m; i++) {
+        float re = (float)pts[2 * i], im = (float)pts[2 * i + 1];
+        e += (float)s_hist[i] * (re * re + im * im);
+      }
+      s_sigma2 = (double)(e / (float)n_sym / (float)a.b_ebn0);
+    }
   }
   __syncthreads();
   const double sigma2 = s_sigma2;
