@@ -37,18 +37,21 @@ def _stale(obj, deps):
     return not os.path.exists(obj) or any(os.path.getmtime(d) > os.path.getmtime(obj) for d in deps)
 
 
-def build(verbose=False, extra_flags=()):
-    os.makedirs(OUT_DIR, exist_ok=True)
+def build(verbose=False, extra_flags=(), out_dir=None, lib=None):
+    """Compile (only stale objects) and link; out_dir/lib override the build paths."""
+    OUT = out_dir or OUT_DIR
+    LIBP = lib or LIB
+    os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     headers.append(os.path.join(HERE, "..", "include", "comrs_gb300.h"))
     jobs = []
     for f in CU:
-        src, obj = os.path.join(CSRC, f), os.path.join(OUT_DIR, f + ".o")
+        src, obj = os.path.join(CSRC, f), os.path.join(OUT, f + ".o")
         if _stale(obj, [src] + headers):
             jobs.append([nvcc, *NVCC_FLAGS, *extra_flags, "-c", src, "-o", obj])
     for f in CPP:
-        src, obj = os.path.join(CSRC, f), os.path.join(OUT_DIR, f + ".o")
+        src, obj = os.path.join(CSRC, f), os.path.join(OUT, f + ".o")
         if _stale(obj, [src] + headers):
             jobs.append(["g++", *CXX_FLAGS, "-c", src, "-o", obj])
 
@@ -62,10 +65,10 @@ def build(verbose=False, extra_flags=()):
 
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
-    objs = [os.path.join(OUT_DIR, f + ".o") for f in CU + CPP]
-    if jobs or not os.path.exists(LIB):
-        run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
-    return LIB
+    objs = [os.path.join(OUT, f + ".o") for f in CU + CPP]
+    if jobs or not os.path.exists(LIBP):
+        run([nvcc, *ARCH, "-shared", "-o", LIBP, *objs, "-lcudart"])
+    return LIBP
 
 
 if __name__ == "__main__":

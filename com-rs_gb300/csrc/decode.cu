@@ -66,18 +66,73 @@ __device__ __forceinline__ int lifted_col(uint32_t entry, int r, int z) {
   return (int)(entry >> 16) * z + c;
 }
 
-// Whether some check of the codeword fails on the hard decisions of post
-// (hard_decisions_are_a_codeword, ldpc.rs:555-557).  Block-wide.
+// ---- syndrome test on packed hard decisions
+// hd holds, per base column j, the hard decisions of its Z bits packed 32 per word
+// (ceil(Z/32) words, then one zero word).  The parity of the 32 lifted rows
+// [32g, 32g + 32) of layer L is the XOR over the layer's entries (j, s) of the
+// Z-bit circular window of column j starting at (32g + s) mod Z.
 template <typename T>
-__device__ __forceinline__ bool some_check_fails(const cbd::DevCode& c, const T* post, int tid) {
-  int bad = 0;
-  if (tid < c.z) {
-    for (int L = 0; L < c.rows_n && !bad; L++) {
-      int par = 0;
-      for (int t = c.layer_start[L]; t < c.layer_start[L + 1]; t++)
-        par ^= (int)(post[lifted_col(c.entry[t], tid, c.z)] < (T)0);
-      bad = par;
+__device__ __forceinline__ void build_hard_decisions(const T* post, uint32_t* hd, int ncol, int z, int tid, int nt) {
+  const int wz = (z + 31) >> 5, ws = wz + 1;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int task = warp; task < ncol * wz; task += nw) {
+    const int j = task / wz, w = task - j * wz;
+    const int r = w * 32 + lane;
+    const uint32_t word = __ballot_sync(0xffffffffu, r < z && post[j * z + r] < (T)0);
+    if (lane == 0) {
+      hd[j * ws + w] = word;
+      if (w == wz - 1) hd[j * ws + wz] = 0u;
     }
+  }
+}
+
+// 32 bits of a packed column from bit o (bits at or beyond Z read as 0)
+__device__ __forceinline__ uint32_t window32(const uint32_t* col, int o) {
+  return __funnelshift_r(col[o >> 5], col[(o >> 5) + 1], o & 31);
+}
+
+// Whether some check fails on the hard decisions of post (hard_decisions_are_a_codeword,
+// ldpc.rs:555-557).  Block-wide.  Stage 1 reads the rows of the first two layers
+// directly (each thread its own row, stopping at the first failure): while the
+// decoder has not converged this almost always finds a failing check.  Only when every
+// one of those rows is satisfied does stage 2 test all rows on packed hard decisions.
+// Either way the answer is exactly "H c != 0".
+template <typename T>
+__device__ __forceinline__ bool some_check_fails(const T* post, uint32_t* hd, const uint32_t* ent,
+                                                 const uint16_t* lstart, int rows_n, int ncol, int z, int tid,
+                                                 int nt) {
+  int bad = 0;
+  if (tid < z) {
+    for (int L = 0; L < 2 && !bad; L++) {
+      uint32_t par = 0;
+      for (int t = lstart[L]; t < lstart[L + 1]; t++) {
+        const uint32_t en = ent[t];
+        int cc = tid + (int)(en & 0xffffu);
+        cc -= (cc >= z) ? z : 0;
+        par ^= (uint32_t)(post[(int)(en >> 16) * z + cc] < (T)0);
+      }
+      bad = (int)par;
+    }
+  }
+  if (__syncthreads_or(bad)) return true;
+  build_hard_decisions(post, hd, ncol, z, tid, nt);
+  __syncthreads();
+  const int wz = (z + 31) >> 5, ws = wz + 1;
+  for (int task = tid; task < rows_n * wz && !bad; task += nt) {
+    const int L = task / wz, g = task - L * wz;
+    const int r0 = g * 32, nrows = min(32, z - r0);
+    uint32_t par = 0;
+    for (int t = lstart[L]; t < lstart[L + 1]; t++) {
+      const uint32_t en = ent[t];
+      const uint32_t* col = hd + (en >> 16) * ws;
+      int o = r0 + (int)(en & 0xffffu);
+      o -= (o >= z) ? z : 0;
+      uint32_t win = window32(col, o);
+      if (o + nrows > z) win |= window32(col, 0) << (z - o);
+      par ^= win;
+    }
+    const uint32_t mask = nrows == 32 ? 0xffffffffu : ((1u << nrows) - 1u);
+    bad = (par & mask) != 0u;
   }
   return __syncthreads_or(bad) != 0;
 }
@@ -135,9 +190,86 @@ __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t*
   }
 }
 
+// f32 row update with fewer integer-pipe operations (same results as row_update for
+// finite LLRs):
+//   * min and second min with min/max only; the edges that receive the second minimum
+//     are those whose magnitude equals the minimum (if several do, the two minima are
+//     equal, so every edge gets the same magnitude, as in the reference);
+//   * the sign test `x < 0` is the sign bit of x: the posteriors never hold -0.0 (they
+//     start as 0.0 + LLR or 30.0, and a difference or sum is -0.0 only when an operand
+//     already is), so no message input x = post - c2v is -0.0 either;
+//   * outgoing signs are applied and collected with bit operations.
+// State word: bits 0-4 an edge holding the second minimum, bits 8.. the outgoing sign of
+// edge e at bit 8 + (D - 1 - e).
+template <int D>
+__device__ __forceinline__ void row_update_lean(float* __restrict__ post, const uint32_t* __restrict__ ent, int r,
+                                                int z, float a1, float a2, uint32_t mt, int rule, float alpha,
+                                                float& n1, float& n2, uint32_t& nm) {
+  int off[D];
+  float x[D];
+  const int old_i1 = (int)(mt & 31u);
+  const uint32_t t0 = mt << (24 - D);  // the old sign of edge 0 at bit 31
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    const uint32_t en = ent[e];
+    unsigned c = (unsigned)r + (en & 0xffffu);
+    unsigned cm = c - (unsigned)z;
+    off[e] = (int)(en >> 16) * z + (int)min(c, cm);
+    float mag = (e == old_i1) ? a2 : a1;
+    uint32_t ob = __float_as_uint(mag) | ((t0 << e) & 0x80000000u);
+    x[e] = __fsub_rn(post[off[e]], __uint_as_float(ob));
+  }
+  uint32_t par = 0;
+  float m1 = infinity<float>(), m2 = infinity<float>();
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    par ^= __float_as_uint(x[e]);
+    float av = fabsf(x[e]);
+    m2 = fminf(m2, fmaxf(m1, av));
+    m1 = fminf(m1, av);
+  }
+  if (rule == cbd::RULE_NMS) {
+    n1 = __fmul_rn(alpha, m1);
+    n2 = __fmul_rn(alpha, m2);
+  } else {
+    n1 = fmaxf(__fsub_rn(m1, alpha), 0.0f);
+    n2 = fmaxf(__fsub_rn(m2, alpha), 0.0f);
+  }
+  const uint32_t ps = par & 0x80000000u;
+  const uint32_t n1p = __float_as_uint(n1) | ps, n2p = __float_as_uint(n2) | ps;
+  uint32_t sm = 0;
+  int i1 = 0;
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    bool eq = fabsf(x[e]) == m1;
+    uint32_t magp = eq ? n2p : n1p;
+    i1 = eq ? e : i1;
+    uint32_t ob = magp ^ (__float_as_uint(x[e]) & 0x80000000u);
+    post[off[e]] = __fadd_rn(x[e], __uint_as_float(ob));
+    sm = (sm << 1) | (ob >> 31);
+  }
+  nm = (sm << 8) | (uint32_t)i1;
+}
+
 template <typename T>
 __device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent, int r, int z, T a1, T a2,
                                              uint32_t mt, int rule, T alpha, T& n1, T& n2, uint32_t& nm) {
+#ifndef CB_F32_CLASSIC_ROWS
+  if constexpr (sizeof(T) == 4) {
+    switch (d) {
+      case 3: row_update_lean<3>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 4: row_update_lean<4>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 5: row_update_lean<5>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 6: row_update_lean<6>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 7: row_update_lean<7>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 8: row_update_lean<8>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 9: row_update_lean<9>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 10: row_update_lean<10>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      default: row_update_lean<19>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    }
+    return;
+  }
+#endif
   switch (d) {
     case 3: row_update<T, 3>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
     case 4: row_update<T, 4>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
@@ -151,25 +283,81 @@ __device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent
   }
 }
 
+// check-node state of one lifted row: f32 as one 16-byte record {n1, n2, meta, 0};
+// f64 as a 16-byte {n1, n2} record plus a separate plane of meta words
 template <typename T>
-__global__ void __launch_bounds__(384) layered_kernel(const __grid_constant__ DecodeArgs<T> a) {
+struct StateSlot;
+template <>
+struct StateSlot<float> {
+  uint4* rec;
+  __device__ __forceinline__ StateSlot(unsigned char* base, int rows) : rec(reinterpret_cast<uint4*>(base)) { (void)rows; }
+  __device__ __forceinline__ void load(int row, float& a1, float& a2, uint32_t& mt) const {
+    uint4 v = rec[row];
+    a1 = __uint_as_float(v.x);
+    a2 = __uint_as_float(v.y);
+    mt = v.z;
+  }
+  __device__ __forceinline__ void store(int row, float n1, float n2, uint32_t nm) const {
+    rec[row] = make_uint4(__float_as_uint(n1), __float_as_uint(n2), nm, 0u);
+  }
+  static __host__ __device__ size_t bytes(int rows) { return (size_t)rows * 16; }
+};
+template <>
+struct StateSlot<double> {
+  double2* rec;
+  uint32_t* meta;
+  __device__ __forceinline__ StateSlot(unsigned char* base, int rows)
+      : rec(reinterpret_cast<double2*>(base)), meta(reinterpret_cast<uint32_t*>(base + (size_t)rows * 16)) {}
+  __device__ __forceinline__ void load(int row, double& a1, double& a2, uint32_t& mt) const {
+    double2 v = rec[row];
+    a1 = v.x;
+    a2 = v.y;
+    mt = meta[row];
+  }
+  __device__ __forceinline__ void store(int row, double n1, double n2, uint32_t nm) const {
+    rec[row] = make_double2(n1, n2);
+    meta[row] = nm;
+  }
+  static __host__ __device__ size_t bytes(int rows) { return (size_t)rows * 20; }
+};
+
+template <typename T>
+__host__ __device__ __forceinline__ size_t slot_bytes(int rows) {
+  return (StateSlot<T>::bytes(rows) + 255) & ~(size_t)255;
+}
+
+template <typename T>
+__host__ __device__ __forceinline__ size_t decode_smem_bytes(int n_full, int z, int rows_n, int n_entries) {
+  const int ws = (z + 31) / 32 + 1;
+  size_t b = (size_t)n_full * sizeof(T);
+  b += (size_t)(n_full / z) * ws * 4;    // packed hard decisions
+  b += (size_t)n_entries * 4;             // entries
+  b += (size_t)(rows_n + 1) * 2 + 16;     // layer starts
+  return (b + 15) & ~(size_t)15;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(const __grid_constant__ DecodeArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  T* post = reinterpret_cast<T*>(smem);
-  __shared__ long long s_cw;
-  __shared__ unsigned int s_err;
   const cbd::DevCode& c = a.code;
   const int z = c.z, nt = blockDim.x, tid = threadIdx.x;
+  const int ncol = c.n_full / z;
+  const int ws = (z + 31) / 32 + 1;
+  T* post = reinterpret_cast<T*>(smem);
+  uint32_t* hd = reinterpret_cast<uint32_t*>(post + c.n_full);
+  uint32_t* s_ent = hd + ncol * ws;
+  uint16_t* s_lstart = reinterpret_cast<uint16_t*>(s_ent + c.n_entries);
+  __shared__ long long s_cw;
+  __shared__ unsigned int s_err;
   const int rows = c.rows_n * z;
-  const size_t slot = ((size_t)rows * (2 * sizeof(T) + 4) + 255) & ~(size_t)255;
-  unsigned char* base = reinterpret_cast<unsigned char*>(a.state) + (size_t)blockIdx.x * slot;
-  T* A1 = reinterpret_cast<T*>(base);
-  T* A2 = A1 + rows;
-  uint32_t* meta = reinterpret_cast<uint32_t*>(A2 + rows);
+  const StateSlot<T> st(reinterpret_cast<unsigned char*>(a.state) + (size_t)blockIdx.x * slot_bytes<T>(rows), rows);
   const T alpha = (T)a.cfg.alpha;
   const int rule = a.cfg.rule;
   const int max_it = a.cfg.max_iterations;
   const int wpf = (c.k_info + 31) >> 5;
   const bool active = tid < z;
+  for (int i = tid; i < c.n_entries; i += nt) s_ent[i] = c.entry[i];
+  for (int i = tid; i <= c.rows_n; i += nt) s_lstart[i] = c.layer_start[i];
 
   for (;;) {
     if (tid == 0) {
@@ -203,43 +391,31 @@ __global__ void __launch_bounds__(384) layered_kernel(const __grid_constant__ De
 
     // ---- propagate (ldpc.rs:509-551), layered schedule
     int it = 0;
-    if (some_check_fails(c, post, tid)) {
+    if (some_check_fails(post, hd, s_ent, s_lstart, c.rows_n, ncol, z, tid, nt)) {
       it = max_it;
       for (int iter = 1; iter <= max_it; iter++) {
         // the state of a layer is prefetched one layer ahead
         T a1 = (T)0, a2 = (T)0;
         uint32_t mt = 0;
-        if (iter > 1 && active) {
-          a1 = A1[tid];
-          a2 = A2[tid];
-          mt = meta[tid];
-        }
+        if (iter > 1 && active) st.load(tid, a1, a2, mt);
         for (int L = 0; L < c.rows_n; L++) {
           T p1 = (T)0, p2 = (T)0;
           uint32_t pm = 0;
-          if (iter > 1 && active && L + 1 < c.rows_n) {
-            const int nrow = (L + 1) * z + tid;
-            p1 = A1[nrow];
-            p2 = A2[nrow];
-            pm = meta[nrow];
-          }
+          if (iter > 1 && active && L + 1 < c.rows_n) st.load((L + 1) * z + tid, p1, p2, pm);
           if (active) {
             const int s0 = c.layer_start[L];
             const int d = c.layer_start[L + 1] - s0;
             T n1, n2;
             uint32_t nm;
             row_dispatch<T>(d, post, c.entry + s0, tid, z, a1, a2, mt, rule, alpha, n1, n2, nm);
-            const int row = L * z + tid;
-            A1[row] = n1;
-            A2[row] = n2;
-            meta[row] = nm;
+            st.store(L * z + tid, n1, n2, nm);
           }
           a1 = p1;
           a2 = p2;
           mt = pm;
           __syncthreads();
         }
-        if (!some_check_fails(c, post, tid)) {
+        if (!some_check_fails(post, hd, s_ent, s_lstart, c.rows_n, ncol, z, tid, nt)) {
           it = iter;
           break;
         }
@@ -289,14 +465,15 @@ void* kernel_for(int max_degree) {
 int block_threads(int z) { return ((z + 31) / 32) * 32; }
 
 size_t smem_bytes(const cbd::DevCode& c, int precision) {
-  return (size_t)c.n_full * (precision == 0 ? sizeof(double) : sizeof(float));
+  return precision == 0 ? decode_smem_bytes<double>(c.n_full, c.z, c.rows_n, c.n_entries)
+                        : decode_smem_bytes<float>(c.n_full, c.z, c.rows_n, c.n_entries);
 }
 
 }  // namespace
 
 size_t decode_state_bytes_per_slot(const cbd::DevCode& c, int precision) {
-  size_t t = precision == 0 ? sizeof(double) : sizeof(float);
-  return (((size_t)c.rows_n * c.z * (2 * t + 4)) + 255) & ~(size_t)255;
+  const int rows = c.rows_n * c.z;
+  return precision == 0 ? slot_bytes<double>(rows) : slot_bytes<float>(rows);
 }
 
 int decode_grid_size(const cbd::DevCode& c, int precision, int device) {
