@@ -64,6 +64,7 @@ SYMBOLS = [
     ("cb_generate_frames", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp]),
     ("cb_run_frames_device", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp]),
     ("cb_generate_frames_device", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp, _vp]),
+    ("cb_decode_device_noalloc", _i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
     ("cb_xoshiro_jump", _i32, [_vp, _u64, _vp]),
 ]
 

@@ -591,3 +591,86 @@ cb_status cb_xoshiro_jump(const uint64_t state[4], uint64_t steps, uint64_t out[
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- decode without allocation
+// Some callers cannot call cudaMalloc: a host framework that owns every byte of device
+// memory through its own pool, or a real-time loop that forbids allocation once it has
+// started (a cudaMalloc may block and synchronise the device).  For them
+// cb_decode_device_noalloc keeps the decoder's scratch (its work counter and the
+// check-node state of each resident CTA) in this file-scope array, which every GPU that
+// loads the library holds until the process exits.
+constexpr size_t kNoallocScratchBytes = (size_t)32 << 20;  // 32 MiB
+constexpr size_t kNoallocCounterBytes = 256;
+constexpr int kNoallocMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+// The device address of the scratch array on `device` (the current device).  In host
+// code the array's name is only a host-side stand-in, so the address comes from
+// cudaGetSymbolAddress, once per device.
+cb_status noalloc_scratch(cb_code* c, int device, void** out) {
+  if (device < 0 || device >= kNoallocMaxDevices) return fail(c, CB_ERR_CONFIG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_ptr[device] = p;
+  }
+  *out = g_noalloc_ptr[device];
+  return CB_OK;
+}
+
+template <typename T>
+cb_status decode_noalloc_impl(cb_code* c, void* scratch, const T* llr, int64_t n, uint32_t* bits, int32_t* iters,
+                              cudaStream_t s) {
+  const size_t slot = cbk::decode_state_bytes_per_slot(c->dev, c->precision);
+  const int64_t fit = (int64_t)((kNoallocScratchBytes - kNoallocCounterBytes) / slot);
+  if (fit < 1)
+    return fail(c, CB_ERR_SHAPE,
+                "the check-node state of one CTA (" + std::to_string(slot) + " bytes) exceeds the " +
+                    std::to_string(kNoallocScratchBytes >> 20) + " MiB scratch of cb_decode_device_noalloc");
+  const int occupancy = cbk::decode_grid_size(c->dev, c->precision, c->device);
+  if (occupancy <= 0) return fail(c, CB_ERR_CUDA, "the decoder does not fit an SM (occupancy 0)");
+  cbk::DecodeArgs<T> a;
+  a.code = c->dev;
+  a.cfg = c->cfg;
+  a.llr = llr;
+  a.n_frames = n;
+  a.bits_out = bits;
+  a.app_out = nullptr;
+  a.post_out = nullptr;
+  a.iters_out = iters;
+  a.ref_bits = nullptr;
+  a.results = nullptr;
+  a.work_counter = reinterpret_cast<int32_t*>(scratch);
+  a.state = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(scratch) + kNoallocCounterBytes);
+  a.status = nullptr;
+  // the work counter must start at zero; the state slots need no clearing (the first
+  // iteration of every codeword reads no state)
+  CB_CUDA(c, cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), s));
+  const int grid = (int)std::min<int64_t>(std::min<int64_t>(occupancy, fit), n);
+  CB_CUDA(c, cbk::launch_decode<T>(a, grid, s));
+  return CB_OK;
+}
+}  // namespace
+
+extern "C" cb_status cb_decode_device_noalloc(cb_code* c, const void* llr, int64_t n, uint32_t* bits,
+                                              int32_t* iters, void* stream) {
+  if (!c || !llr || n < 0) return fail(c, CB_ERR_CONFIG, "NULL argument or negative count");
+  if (!c->host.map_is_offset)
+    return fail(c, CB_ERR_CONFIG,
+                "cb_decode_device_noalloc needs the plain rate matching (rv 0, Qm 1, no filler bits sent)");
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (n == 0) return CB_OK;
+  void* scratch = nullptr;
+  if (cb_status st = noalloc_scratch(c, c->device, &scratch)) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (c->precision == CB_F64)
+    return decode_noalloc_impl<double>(c, scratch, (const double*)llr, n, bits, iters, s);
+  return decode_noalloc_impl<float>(c, scratch, (const float*)llr, n, bits, iters, s);
+}

@@ -133,6 +133,22 @@ cb_status cb_generate_frames_device(cb_code* code, int32_t modulation_order, uin
                                     uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,
                                     void* llr_dev, uint32_t* info_dev, void* stream);
 
+/* cb_decode_device for callers that cannot allocate device memory (a host framework
+ * that owns all device memory through its own pool, or a real-time loop that forbids
+ * cudaMalloc after start-up).  No counterpart in the reference: it is an addition of
+ * this library.  Calls no cudaMalloc, cudaFree or allocating library routine: its
+ * scratch (work counter and per-CTA check-node state) is a static 32 MiB device array
+ * that every GPU loading the library holds until exit.  The first call on a device
+ * looks up that array's device address; make that first call before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU (two streams,
+ * two threads) race: serialise them.  Codes whose per-CTA state exceeds the array
+ * (CB_ERR_SHAPE) or whose rate matching is not the plain offset 2Z + t (rv 0, Qm 1, no
+ * filler bits sent; CB_ERR_CONFIG) are rejected.  Fewer CTAs run when the state of
+ * all resident CTAs does not fit, so large codes decode more slowly than with
+ * cb_decode_device.  Outputs as cb_decode_device. */
+cb_status cb_decode_device_noalloc(cb_code* code, const void* llr_dev, int64_t n_frames, uint32_t* bits_dev,
+                                   int32_t* iterations_dev, void* stream);
+
 /* The state of the xoshiro256** generator after `steps` draws from `state` (jump-ahead
  * by a polynomial; Rng::state / Rng::from_state, crates/com-core/src/rng.rs:83-96). */
 cb_status cb_xoshiro_jump(const uint64_t state[4], uint64_t steps, uint64_t out[4]);
