@@ -157,14 +157,25 @@ class Grid:
         return out
 
 
-def run(code, grid, stop, seed=0, name="bicm_ldpc", batch=32, modulation=4, on_batch=None):
+def run(code, grid, stop, seed=0, name="bicm_ldpc", batch=32, modulation=4, on_batch=None, rank=0, world=1,
+        all_reduce=None):
     """A campaign of `code` (an NrLdpc) over `grid` (conditions with ``ebn0_db``).
 
     Returns one ConditionResult per condition with the metrics ``ber``, ``fer``
     (ErrorRate) and ``iterations`` (Mean).
+
+    Several processes (one GPU each) run one campaign together: with ``world`` > 1
+    every batch is split into ``world`` contiguous frame ranges, process ``rank`` runs
+    its own, and ``all_reduce`` (a function summing an int64 numpy vector over the
+    processes, e.g. over torch.distributed) merges the integer counts before the stop
+    rule is evaluated.  The result equals the one-process campaign with the same batch.
     """
+    import numpy as np
+
     if not stop.is_bounded():
         raise ValueError("the stopping rule can run forever: add Stop.max_trials with or_")
+    if world > 1 and all_reduce is None:
+        raise ValueError("a multi-process campaign needs all_reduce")
     batch = max(1, int(batch))
     results = []
     for index, cond in enumerate(grid.conditions()):
@@ -174,10 +185,18 @@ def run(code, grid, stop, seed=0, name="bicm_ldpc", batch=32, modulation=4, on_b
         limit = stop.trial_limit()
         while True:
             end = trials + batch if limit is None else max(min(trials + batch, limit), trials + 1)
-            fr = code.run_frames(seed, name, index, trials, end - trials, cond["ebn0_db"], modulation)
-            rec["ber"].add(fr["bit_errors"].sum(dtype="u8"), code.k_info * len(fr))
-            rec["fer"].add(fr["frame_error"].sum(dtype="u8"), len(fr))
-            rec["iterations"].add_many(len(fr), fr["iterations"].sum(dtype="u8"))
+            n = end - trials
+            lo, hi = trials + n * rank // world, trials + n * (rank + 1) // world
+            counts = np.zeros(4, np.int64)
+            if hi > lo:
+                fr = code.run_frames(seed, name, index, lo, hi - lo, cond["ebn0_db"], modulation)
+                counts[:] = (fr["bit_errors"].sum(dtype="u8"), fr["frame_error"].sum(dtype="u8"),
+                             fr["iterations"].sum(dtype="u8"), len(fr))
+            if world > 1:
+                counts = all_reduce(counts)
+            rec["ber"].add(counts[0], code.k_info * counts[3])
+            rec["fer"].add(counts[1], counts[3])
+            rec["iterations"].add_many(counts[3], counts[2])
             trials = end
             if on_batch:
                 on_batch(index, trials, rec)
