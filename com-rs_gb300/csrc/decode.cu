@@ -287,18 +287,37 @@ __device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent
 // f64 as a 16-byte {n1, n2} record plus a separate plane of meta words
 template <typename T>
 struct StateSlot;
+// The state records of all resident CTAs (86 MB at BG1 Z = 384) fit in L2, but the LLR
+// stream of a launch (830 MB for 8192 codewords) would evict them: the records are read
+// and written with an L2 evict-last policy, the LLRs with streaming loads.
+__device__ __forceinline__ uint64_t l2_evict_last_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
 template <>
 struct StateSlot<float> {
   uint4* rec;
-  __device__ __forceinline__ StateSlot(unsigned char* base, int rows) : rec(reinterpret_cast<uint4*>(base)) { (void)rows; }
+  uint64_t pol;
+  __device__ __forceinline__ StateSlot(unsigned char* base, int rows)
+      : rec(reinterpret_cast<uint4*>(base)), pol(l2_evict_last_policy()) {
+    (void)rows;
+  }
   __device__ __forceinline__ void load(int row, float& a1, float& a2, uint32_t& mt) const {
-    uint4 v = rec[row];
-    a1 = __uint_as_float(v.x);
-    a2 = __uint_as_float(v.y);
-    mt = v.z;
+    uint32_t x, y, zz, w;
+    asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(x), "=r"(y), "=r"(zz), "=r"(w)
+                 : "l"(rec + row), "l"(pol));
+    (void)w;
+    a1 = __uint_as_float(x);
+    a2 = __uint_as_float(y);
+    mt = zz;
   }
   __device__ __forceinline__ void store(int row, float n1, float n2, uint32_t nm) const {
-    rec[row] = make_uint4(__float_as_uint(n1), __float_as_uint(n2), nm, 0u);
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(rec + row),
+                 "r"(__float_as_uint(n1)), "r"(__float_as_uint(n2)), "r"(nm), "r"(0u), "l"(pol)
+                 : "memory");
   }
   static __host__ __device__ size_t bytes(int rows) { return (size_t)rows * 16; }
 };
@@ -373,9 +392,9 @@ __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(co
     for (int v = tid; v < c.n_full; v += nt) post[v] = (T)0;
     __syncthreads();
     if (c.map_is_offset) {
-      for (int t = tid; t < c.e; t += nt) post[2 * z + t] = add_rn((T)0, llr[t]);
+      for (int t = tid; t < c.e; t += nt) post[2 * z + t] = add_rn((T)0, __ldcs(llr + t));
     } else if (!c.has_repeats) {
-      for (int t = tid; t < c.e; t += nt) post[c.map[t]] = add_rn((T)0, llr[t]);
+      for (int t = tid; t < c.e; t += nt) post[c.map[t]] = add_rn((T)0, __ldcs(llr + t));
     } else {
       for (int v = tid; v < c.n_full; v += nt) {
         int b0 = c.inv_start[v], b1 = c.inv_start[v + 1];
