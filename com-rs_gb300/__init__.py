@@ -64,6 +64,15 @@ SYMBOLS = [
     ("cb_generate_frames", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp]),
     ("cb_run_frames_device", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp]),
     ("cb_generate_frames_device", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp, _vp]),
+    ("cb_nms_create", _i32, [_vp, _i32, _i32, C.POINTER(_vp)]),
+    ("cb_nms_destroy", None, [_vp]),
+    ("cb_nms_info", _i32, [_vp, _vp]),
+    ("cb_nms_get_weights", _i32, [_vp, _vp, _vp]),
+    ("cb_nms_set_weights", _i32, [_vp, _vp, _vp]),
+    ("cb_nms_forward", _i32, [_vp, _vp, _i64, _vp]),
+    ("cb_nms_gradients", _i32, [_vp, _vp, _vp, _i64, _i32, _vp, _vp, C.POINTER(_dbl)]),
+    ("cb_nms_train_step", _i32, [_vp, _i32, _u64, _u64, _i64, _dbl, _dbl, _dbl, _i32, C.POINTER(_dbl)]),
+    ("cb_nms_run_frames", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp]),
     ("cb_decode_device_noalloc", _i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
     ("cb_xoshiro_jump", _i32, [_vp, _u64, _vp]),
 ]
@@ -239,3 +248,79 @@ class NrLdpc:
         _check(lib().cb_generate_frames(self._h, modulation, seed, nh, condition, first_frame, n_frames, ebn0_db,
                                         _p(llr), _p(info)), self._h)
         return llr, info
+
+
+class LearnedNms:
+    """The learned (neural) min-sum on an f32 NrLdpc: per-iteration scales and offsets,
+    one per lifted edge or, with ``shared``, one per base-graph edge; starts as the
+    plain normalised min-sum (its fallback)."""
+
+    def __init__(self, code, iterations, shared=False):
+        if code.precision != "f32":
+            raise ComrsError(-1, "the learned min-sum runs on an f32 code object")
+        self.code = code
+        h = C.c_void_p()
+        _check(lib().cb_nms_create(code._h, iterations, int(bool(shared)), C.byref(h)), code._h)
+        self._h = h
+        info = np.zeros(4, np.int64)
+        _check(lib().cb_nms_info(h, _p(info)))
+        self.n_weights, self.iterations, self.shared = int(info[0]), int(info[1]), bool(info[2])
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cb_nms_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def steps(self):
+        info = np.zeros(4, np.int64)
+        _check(lib().cb_nms_info(self._h, _p(info)))
+        return int(info[3])
+
+    def weights(self):
+        a, b = np.zeros(self.n_weights, np.float32), np.zeros(self.n_weights, np.float32)
+        _check(lib().cb_nms_get_weights(self._h, _p(a), _p(b)), self.code._h)
+        return a, b
+
+    def set_weights(self, alpha, beta):
+        a = np.ascontiguousarray(alpha, np.float32)
+        b = np.ascontiguousarray(beta, np.float32)
+        if a.size != self.n_weights or b.size != self.n_weights:
+            raise ComrsError(-2, f"{self.n_weights} scales and offsets expected")
+        _check(lib().cb_nms_set_weights(self._h, _p(a), _p(b)), self.code._h)
+
+    def forward(self, llr):
+        x = np.ascontiguousarray(llr, np.float32).reshape(-1, self.code.e)
+        post = np.zeros((x.shape[0], self.code.n_full), np.float32)
+        _check(lib().cb_nms_forward(self._h, _p(x), x.shape[0], _p(post)), self.code._h)
+        return post
+
+    def gradients(self, llr, cw, multi_loss=False):
+        x = np.ascontiguousarray(llr, np.float32).reshape(-1, self.code.e)
+        c = np.ascontiguousarray(cw, np.uint8).reshape(-1, self.code.n_full)
+        ga, gb = np.zeros(self.n_weights, np.float32), np.zeros(self.n_weights, np.float32)
+        loss = C.c_double()
+        _check(lib().cb_nms_gradients(self._h, _p(x), _p(c), x.shape[0], int(multi_loss), _p(ga), _p(gb),
+                                      C.byref(loss)),
+               self.code._h)
+        return loss.value, ga, gb
+
+    def train_step(self, seed, name, batch, ebn0_lo, ebn0_hi, lr, modulation=4, multi_loss=True):
+        loss = C.c_double()
+        nh = fnv1a64(name) if isinstance(name, (str, bytes)) else int(name)
+        _check(lib().cb_nms_train_step(self._h, modulation, seed, nh, batch, ebn0_lo, ebn0_hi, lr, int(multi_loss),
+                                       C.byref(loss)),
+               self.code._h)
+        return loss.value
+
+    def run_frames(self, seed, name, condition, first_frame, n_frames, ebn0_db, modulation=4):
+        out = np.zeros(n_frames, FRAME_DTYPE)
+        nh = fnv1a64(name) if isinstance(name, (str, bytes)) else int(name)
+        _check(lib().cb_nms_run_frames(self._h, modulation, seed, nh, condition, first_frame, n_frames, ebn0_db,
+                                       _p(out)), self.code._h)
+        return out

@@ -193,7 +193,8 @@ cb_status gen_config(cb_code* c, int m, GenCache** out) {
 
 template <typename T>
 cb_status gen_device(cb_code* c, GenCache* g, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first,
-                     int64_t n, double ebn0_db, T* llr, uint32_t* info, cudaStream_t s) {
+                     int64_t n, double ebn0_db, T* llr, uint32_t* info, cudaStream_t s,
+                     const float* ebn0_frames = nullptr, uint32_t* cw_out = nullptr) {
   cbk::GenArgs<T> a;
   a.code = c->dev;
   a.m = g->m;
@@ -215,6 +216,9 @@ cb_status gen_device(cb_code* c, GenCache* g, uint64_t seed, uint64_t name_hash,
   a.n_pad = g->n_pad;
   a.llr_out = llr;
   a.info_out = info;
+  a.ebn0_frames = ebn0_frames;
+  a.b_bits = b;
+  a.cw_out = cw_out;
   CB_CUDA(c, cbk::launch_gen<T>(a, s));
   return CB_OK;
 }
@@ -587,6 +591,268 @@ cb_status cb_xoshiro_jump(const uint64_t state[4], uint64_t steps, uint64_t out[
   uint64_t s[4] = {state[0], state[1], state[2], state[3]};
   cbh::xoshiro_apply_jump(s, cbh::xoshiro_jump_poly(steps));
   std::memcpy(out, s, sizeof s);
+  return CB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- learned min-sum
+struct cb_nms {
+  cb_code* code = nullptr;
+  int T = 0, shared = 0, step = 0;
+  int64_t nw = 0;        // weights per kind (scales, offsets)
+  float* d_w = nullptr;  // [2 nw]: scales then offsets
+  float* d_g = nullptr;
+  float* d_m = nullptr;
+  float* d_v = nullptr;
+  float* d_X = nullptr;
+  size_t X_cap = 0;
+  float* d_P = nullptr;
+  size_t P_cap = 0;
+  float* d_c2v = nullptr;
+  size_t c2v_cap = 0;
+  float* d_post = nullptr;
+  size_t post_cap = 0;
+  float* d_llr = nullptr;
+  size_t llr_cap = 0;
+  uint32_t* d_cw = nullptr;
+  size_t cw_cap = 0;
+  uint32_t* d_info = nullptr;
+  size_t info_cap = 0;
+  float* d_ebn0 = nullptr;
+  size_t ebn0_cap = 0;
+  float* d_loss = nullptr;
+  cbd::FrameResult* d_res = nullptr;
+  size_t res_cap = 0;
+  std::vector<uint32_t> h_words;
+};
+
+namespace {
+
+cb_status nms_buffers(cb_nms* h, int64_t n, bool train) {
+  cb_code* c = h->code;
+  const size_t edges = (size_t)c->dev.n_entries * c->dev.z;
+  CB_CUDA(c, grow(h->d_c2v, h->c2v_cap, (size_t)n * edges * 4));
+  CB_CUDA(c, grow(h->d_llr, h->llr_cap, (size_t)n * c->host.e * 4));
+  CB_CUDA(c, grow(h->d_post, h->post_cap, (size_t)n * c->host.n_full * 4));
+  CB_CUDA(c, grow(h->d_info, h->info_cap, (size_t)n * ((c->host.k_info + 31) / 32) * 4));
+  CB_CUDA(c, grow(h->d_res, h->res_cap, (size_t)n * sizeof(cbd::FrameResult)));
+  if (train) {
+    CB_CUDA(c, grow(h->d_X, h->X_cap, (size_t)n * h->T * edges * 4));
+    CB_CUDA(c, grow(h->d_P, h->P_cap, (size_t)n * h->T * c->host.n_full * 4));
+    CB_CUDA(c, grow(h->d_cw, h->cw_cap, (size_t)n * ((c->host.n_full + 31) / 32) * 4));
+    CB_CUDA(c, grow(h->d_ebn0, h->ebn0_cap, (size_t)n * 4));
+  }
+  return CB_OK;
+}
+
+cbk::LearnedArgs nms_args(cb_nms* h, int64_t n) {
+  cbk::LearnedArgs a{};
+  a.code = h->code->dev;
+  a.T = h->T;
+  a.shared = h->shared;
+  a.early_stop = 0;
+  a.alpha = h->d_w;
+  a.beta = h->d_w + h->nw;
+  a.llr = h->d_llr;
+  a.n_frames = n;
+  a.c2v = h->d_c2v;
+  a.post_out = h->d_post;
+  a.g_alpha = h->d_g;
+  a.g_beta = h->d_g + h->nw;
+  return a;
+}
+
+// forward (+ backward) of n frames already in d_llr / d_cw; loss into d_loss
+cb_status nms_fwd_bwd(cb_nms* h, int64_t n, bool backward, int multi, cudaStream_t s) {
+  cb_code* c = h->code;
+  cbk::LearnedArgs a = nms_args(h, n);
+  a.cw_bits = h->d_cw;
+  a.X = backward ? h->d_X : nullptr;
+  a.loss = h->d_loss;
+  a.P = h->d_P;
+  a.multi_loss = multi ? 1 : 0;
+  CB_CUDA(c, cudaMemsetAsync(h->d_loss, 0, sizeof(float), s));
+  CB_CUDA(c, cbk::launch_learned(a, true, s));
+  if (backward) {
+    CB_CUDA(c, cudaMemsetAsync(h->d_g, 0, sizeof(float) * 2 * h->nw, s));
+    CB_CUDA(c, cbk::launch_learned(a, false, s));
+  }
+  return CB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cb_status cb_nms_create(cb_code* c, int32_t iterations, int32_t shared, cb_nms** out) {
+  if (!c || !out) return fail(c, CB_ERR_CONFIG, "NULL argument");
+  *out = nullptr;
+  if (c->precision != CB_F32) return fail(c, CB_ERR_CONFIG, "the learned min-sum runs on an f32 code object");
+  if (iterations < 1 || iterations > 255) return fail(c, CB_ERR_CONFIG, "iterations in 1..255");
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (cb_status st = ensure_device(c)) return st;
+  cb_nms* h = new cb_nms();
+  h->code = c;
+  h->T = iterations;
+  h->shared = shared ? 1 : 0;
+  h->nw = (int64_t)iterations * c->dev.n_entries * (shared ? 1 : c->dev.z);
+  std::vector<float> w(2 * h->nw, 0.f);
+  for (int64_t i = 0; i < h->nw; i++) w[i] = (float)c->cfg.alpha;  // the plain min-sum
+  cudaError_t e = cudaMalloc(&h->d_w, sizeof(float) * 2 * h->nw);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_g, sizeof(float) * 2 * h->nw);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_m, sizeof(float) * 2 * h->nw);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_v, sizeof(float) * 2 * h->nw);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_loss, 64);
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_w, w.data(), sizeof(float) * 2 * h->nw, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(h->d_m, 0, sizeof(float) * 2 * h->nw);
+  if (e == cudaSuccess) e = cudaMemset(h->d_v, 0, sizeof(float) * 2 * h->nw);
+  if (e != cudaSuccess) {
+    cb_nms_destroy(h);
+    return cuda_fail(c, e, "cb_nms_create");
+  }
+  *out = h;
+  return CB_OK;
+}
+
+void cb_nms_destroy(cb_nms* h) {
+  if (!h) return;
+  cudaSetDevice(h->code->device);
+  void* bufs[] = {h->d_w, h->d_g, h->d_m, h->d_v, h->d_X, h->d_P, h->d_c2v, h->d_post, h->d_llr, h->d_cw, h->d_info,
+                  h->d_ebn0, h->d_loss, h->d_res};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  delete h;
+}
+
+cb_status cb_nms_info(const cb_nms* h, int64_t info[4]) {
+  if (!h || !info) return fail(nullptr, CB_ERR_CONFIG, "NULL argument");
+  info[0] = h->nw;
+  info[1] = h->T;
+  info[2] = h->shared;
+  info[3] = h->step;
+  return CB_OK;
+}
+
+cb_status cb_nms_get_weights(cb_nms* h, float* alpha, float* beta) {
+  if (!h) return fail(nullptr, CB_ERR_CONFIG, "NULL argument");
+  cb_code* c = h->code;
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (alpha) CB_CUDA(c, cudaMemcpy(alpha, h->d_w, sizeof(float) * h->nw, cudaMemcpyDeviceToHost));
+  if (beta) CB_CUDA(c, cudaMemcpy(beta, h->d_w + h->nw, sizeof(float) * h->nw, cudaMemcpyDeviceToHost));
+  return CB_OK;
+}
+
+cb_status cb_nms_set_weights(cb_nms* h, const float* alpha, const float* beta) {
+  if (!h || !alpha || !beta) return fail(nullptr, CB_ERR_CONFIG, "NULL argument");
+  cb_code* c = h->code;
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  CB_CUDA(c, cudaMemcpy(h->d_w, alpha, sizeof(float) * h->nw, cudaMemcpyHostToDevice));
+  CB_CUDA(c, cudaMemcpy(h->d_w + h->nw, beta, sizeof(float) * h->nw, cudaMemcpyHostToDevice));
+  CB_CUDA(c, cudaMemset(h->d_m, 0, sizeof(float) * 2 * h->nw));
+  CB_CUDA(c, cudaMemset(h->d_v, 0, sizeof(float) * 2 * h->nw));
+  h->step = 0;
+  return CB_OK;
+}
+
+cb_status cb_nms_forward(cb_nms* h, const float* llr, int64_t n, float* post) {
+  if (!h || !llr || !post || n < 0) return fail(nullptr, CB_ERR_CONFIG, "NULL argument or negative count");
+  cb_code* c = h->code;
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (n == 0) return CB_OK;
+  if (cb_status st = nms_buffers(h, n, false)) return st;
+  CB_CUDA(c, cudaMemcpyAsync(h->d_llr, llr, (size_t)n * c->host.e * 4, cudaMemcpyHostToDevice, c->stream));
+  cbk::LearnedArgs a = nms_args(h, n);
+  CB_CUDA(c, cbk::launch_learned(a, true, c->stream));
+  CB_CUDA(c, cudaMemcpyAsync(post, h->d_post, (size_t)n * c->host.n_full * 4, cudaMemcpyDeviceToHost, c->stream));
+  CB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CB_OK;
+}
+
+cb_status cb_nms_gradients(cb_nms* h, const float* llr, const uint8_t* cw, int64_t n, int32_t multi_loss,
+                           float* g_alpha, float* g_beta, double* loss) {
+  if (!h || !llr || !cw || n <= 0) return fail(nullptr, CB_ERR_CONFIG, "NULL argument or no frames");
+  cb_code* c = h->code;
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (cb_status st = nms_buffers(h, n, true)) return st;
+  const int wpc = (c->host.n_full + 31) / 32;
+  h->h_words.assign((size_t)n * wpc, 0u);
+  for (int64_t f = 0; f < n; f++)
+    for (int v = 0; v < c->host.n_full; v++)
+      if (cw[(size_t)f * c->host.n_full + v] & 1) h->h_words[(size_t)f * wpc + v / 32] |= 1u << (v % 32);
+  CB_CUDA(c, cudaMemcpyAsync(h->d_llr, llr, (size_t)n * c->host.e * 4, cudaMemcpyHostToDevice, c->stream));
+  CB_CUDA(c, cudaMemcpyAsync(h->d_cw, h->h_words.data(), h->h_words.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  if (cb_status st = nms_fwd_bwd(h, n, true, multi_loss, c->stream)) return st;
+  float l = 0.f;
+  CB_CUDA(c, cudaMemcpyAsync(&l, h->d_loss, 4, cudaMemcpyDeviceToHost, c->stream));
+  if (g_alpha) CB_CUDA(c, cudaMemcpyAsync(g_alpha, h->d_g, sizeof(float) * h->nw, cudaMemcpyDeviceToHost, c->stream));
+  if (g_beta)
+    CB_CUDA(c, cudaMemcpyAsync(g_beta, h->d_g + h->nw, sizeof(float) * h->nw, cudaMemcpyDeviceToHost, c->stream));
+  CB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (loss) *loss = (double)l / (double)n;
+  return CB_OK;
+}
+
+cb_status cb_nms_train_step(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_hash, int64_t batch, double lo,
+                            double hi, double lr, int32_t multi_loss, double* loss) {
+  if (!h || batch <= 0 || !(hi >= lo) || !(lr > 0)) return fail(nullptr, CB_ERR_CONFIG, "bad training arguments");
+  cb_code* c = h->code;
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  GenCache* g;
+  if (cb_status st = gen_config(c, m, &g)) return st;
+  if (cb_status st = nms_buffers(h, batch, true)) return st;
+  // per-frame Eb/N0, uniform in [lo, hi], from a SplitMix64 sequence of (seed, step)
+  std::vector<float> eb((size_t)batch);
+  uint64_t st = seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(h->step + 1));
+  for (int64_t i = 0; i < batch; i++)
+    eb[i] = (float)(lo + (hi - lo) * (double)(cbd::splitmix64(st) >> 11) * (1.0 / 9007199254740992.0));
+  CB_CUDA(c, cudaMemcpyAsync(h->d_ebn0, eb.data(), (size_t)batch * 4, cudaMemcpyHostToDevice, c->stream));
+  // training frames: condition 2^64 - 1 of the scenario, frame step * batch + i
+  if (cb_status s2 = gen_device<float>(c, g, seed, name_hash, ~0ull, (uint64_t)h->step * batch, batch, lo, h->d_llr,
+                                       h->d_info, c->stream, h->d_ebn0, h->d_cw))
+    return s2;
+  if (cb_status s3 = nms_fwd_bwd(h, batch, true, multi_loss, c->stream)) return s3;
+  h->step++;
+  CB_CUDA(c, cbk::launch_adam(h->d_w, h->d_g, h->d_m, h->d_v, 2 * h->nw, (float)lr, h->step, c->stream));
+  float l = 0.f;
+  CB_CUDA(c, cudaMemcpyAsync(&l, h->d_loss, 4, cudaMemcpyDeviceToHost, c->stream));
+  CB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (loss) *loss = (double)l / (double)batch;
+  return CB_OK;
+}
+
+cb_status cb_nms_run_frames(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first,
+                            int64_t n, double ebn0_db, cb_frame_result* out) {
+  if (!h || !out || n < 0) return fail(nullptr, CB_ERR_CONFIG, "NULL argument or negative count");
+  cb_code* c = h->code;
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (n == 0) return CB_OK;
+  GenCache* g;
+  if (cb_status st = gen_config(c, m, &g)) return st;
+  const int64_t chunk = 16384;
+  for (int64_t done = 0; done < n; done += chunk) {
+    int64_t cnt = std::min(chunk, n - done);
+    if (cb_status st = nms_buffers(h, cnt, false)) return st;
+    if (cb_status st = gen_device<float>(c, g, seed, name_hash, cond, first + done, cnt, ebn0_db, h->d_llr, h->d_info,
+                                         c->stream))
+      return st;
+    cbk::LearnedArgs a = nms_args(h, cnt);
+    a.early_stop = 1;
+    a.post_out = nullptr;
+    a.ref_bits = h->d_info;
+    a.results = h->d_res;
+    CB_CUDA(c, cbk::launch_learned(a, true, c->stream));
+    CB_CUDA(c, cudaMemcpyAsync(out + done, h->d_res, (size_t)cnt * sizeof(cb_frame_result), cudaMemcpyDeviceToHost,
+                               c->stream));
+  }
+  CB_CUDA(c, cudaStreamSynchronize(c->stream));
   return CB_OK;
 }
 

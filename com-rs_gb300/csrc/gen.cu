@@ -130,6 +130,14 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
     cw[own] = (uint8_t)acc;
   }
   __syncthreads();
+  if (a.cw_out) {  // the full codeword, packed
+    const int lane = tid & 31, warp = tid >> 5, wpc = (c.n_full + 31) >> 5;
+    for (int b0 = warp * 32; b0 < c.n_full; b0 += (NT / 32) * 32) {
+      int v = b0 + lane;
+      uint32_t word = __ballot_sync(0xffffffffu, v < c.n_full && cw[v]);
+      if (lane == 0) a.cw_out[(size_t)frame * wpc + (b0 >> 5)] = word;
+    }
+  }
   // ---- labels, MSB first (bits_to_index, com-math bits.rs:68-70)
   for (int s = tid; s < n_sym; s += NT) {
     int idx = 0;
@@ -151,7 +159,8 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
         e = __dadd_rn(e, __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
       }
       double p = __ddiv_rn(__dadd_rn(0.0, e), (double)n_sym);
-      s_sigma2 = __ddiv_rn(p, a.b_ebn0);
+      double be = a.ebn0_frames ? a.b_bits * pow(10.0, (double)a.ebn0_frames[frame] / 10.0) : a.b_ebn0;
+      s_sigma2 = __ddiv_rn(p, be);
     }
   } else {
     // f32 frames: the label histogram, then the sum over the M labels
@@ -165,7 +174,8 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
         float re = (float)pts[2 * i], im = (float)pts[2 * i + 1];
         e += (float)s_hist[i] * (re * re + im * im);
       }
-      s_sigma2 = (double)(e / (float)n_sym / (float)a.b_ebn0);
+      float be = a.ebn0_frames ? (float)a.b_bits * exp10f(a.ebn0_frames[frame] / 10.0f) : (float)a.b_ebn0;
+      s_sigma2 = (double)(e / (float)n_sym / be);
     }
   }
   __syncthreads();

@@ -47,8 +47,41 @@ struct GenArgs {
   int32_t bits_per_chunk, syms_per_chunk, n_pad;
   T* llr_out;                  // [n_frames][E]
   uint32_t* info_out;          // [n_frames][ceil(K'/32)]
+  // optional: per-frame Eb/N0 (dB; replaces b_ebn0 by b_bits * 10^(Eb/N0 / 10)) and the
+  // full codeword, packed [n_frames][ceil(n_full/32)] (the targets of training)
+  const float* ebn0_frames = nullptr;
+  double b_bits = 0.0;
+  uint32_t* cw_out = nullptr;
 };
 constexpr int kGenThreads = 128;
+
+// Learned min-sum (nms_learned.cu): forward (training or evaluation) and backward.
+struct LearnedArgs {
+  cbd::DevCode code;
+  int32_t T;           // unrolled iterations
+  int32_t shared;      // 1: weights per base-graph edge, 0: per lifted edge
+  int32_t early_stop;  // 1: syndrome stop after each iteration (evaluation)
+  const float* alpha;  // scales, then
+  const float* beta;   // offsets
+  const float* llr;    // [n_frames][E]
+  int64_t n_frames;
+  const uint32_t* cw_bits;  // [n_frames][ceil(n_full/32)] targets (training)
+  float* X;                 // [n_frames][T][edges] saved inputs (training)
+  float* c2v;               // [n_frames][edges] messages, then their gradients
+  float* post_out;          // [n_frames][n_full]
+  float* loss;              // sum over frames of the mean bit loss (training)
+  float* P;                 // [n_frames][T][n_full] posteriors after each iteration (multi-loss)
+  int32_t multi_loss;       // 1: loss of every iteration's output, weight 1/T each
+  float* g_alpha;           // gradients of the mean loss (backward)
+  float* g_beta;
+  const uint32_t* ref_bits;   // evaluation: sent info bits
+  cbd::FrameResult* results;  // evaluation records
+  int32_t* iters_out;
+};
+size_t learned_smem_bytes(const cbd::DevCode& code);
+cudaError_t launch_learned(const LearnedArgs& a, bool forward, cudaStream_t stream);
+cudaError_t launch_adam(float* w, const float* g, float* m, float* v, int64_t n, float lr, int step,
+                        cudaStream_t stream);
 template <typename T>
 cudaError_t launch_gen(const GenArgs<T>& a, cudaStream_t stream);
 

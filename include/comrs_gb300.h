@@ -133,6 +133,39 @@ cb_status cb_generate_frames_device(cb_code* code, int32_t modulation_order, uin
                                     uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,
                                     void* llr_dev, uint32_t* info_dev, void* stream);
 
+/* ---- Learned (neural) min-sum.  No counterpart in the reference: the layered min-sum
+ * of cb_decode with, at iteration t and edge e, the check message
+ * s * max(alpha[t,e] * m - beta[t,e], 0), trained on the GPU by its own forward and
+ * backward kernels.  The plain normalised min-sum (alpha = the code's alpha, beta = 0)
+ * is its starting point and its fallback.  Runs on an f32 code object, which must
+ * outlive it.  Weights are indexed [t][entry][r] (per lifted edge: entry = base-graph
+ * entry in table order, r = lifted row in its layer) or [t][entry] (shared = 1). */
+typedef struct cb_nms cb_nms;
+cb_status cb_nms_create(cb_code* code, int32_t iterations, int32_t shared, cb_nms** out);
+void cb_nms_destroy(cb_nms* nms);
+/* info[0..4): weights per kind, iterations, shared, training steps taken */
+cb_status cb_nms_info(const cb_nms* nms, int64_t info[4]);
+cb_status cb_nms_get_weights(cb_nms* nms, float* alpha, float* beta);
+/* sets the weights and restarts the optimiser */
+cb_status cb_nms_set_weights(cb_nms* nms, const float* alpha, const float* beta);
+/* the n_full posteriors after exactly `iterations` iterations of n frames of E LLRs */
+cb_status cb_nms_forward(cb_nms* nms, const float* llr, int64_t n_frames, float* post);
+/* the mean loss (binary cross-entropy of the soft output against the n_full codeword
+ * bytes `cw`; with multi_loss the mean over the outputs of all iterations, else the
+ * last output) of n frames and its gradients (nullable outputs) */
+cb_status cb_nms_gradients(cb_nms* nms, const float* llr, const uint8_t* cw, int64_t n_frames, int32_t multi_loss,
+                           float* g_alpha, float* g_beta, double* loss);
+/* one Adam step (learning rate lr) on `batch` frames drawn by the frame generator at
+ * Eb/N0 uniform in [ebn0_lo, ebn0_hi] dB (condition 2^64 - 1 of the stream, frames
+ * step * batch + i); the batch's mean loss before the step into *loss */
+cb_status cb_nms_train_step(cb_nms* nms, int32_t modulation_order, uint64_t seed, uint64_t name_hash,
+                            int64_t batch, double ebn0_lo, double ebn0_hi, double lr, int32_t multi_loss,
+                            double* loss);
+/* cb_run_frames with the learned decoder (syndrome stop after each iteration) */
+cb_status cb_nms_run_frames(cb_nms* nms, int32_t modulation_order, uint64_t seed, uint64_t name_hash,
+                            uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,
+                            cb_frame_result* out);
+
 /* cb_decode_device for callers that cannot allocate device memory (a host framework
  * that owns all device memory through its own pool, or a real-time loop that forbids
  * cudaMalloc after start-up).  No counterpart in the reference: it is an addition of

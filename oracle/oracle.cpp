@@ -651,6 +651,137 @@ static void encode_sums(const Code& c, const uint8_t* u, uint8_t* cw) {
   }
 }
 
+
+// ------------------------------------------------------------------ learned min-sum
+// Test oracle of this project's neural min-sum (no counterpart in the reference): the
+// layered min-sum of propagate() with, at iteration t and edge e, the check message
+//   y_e = s_e * max(alpha[t, e] * m_e - beta[t, e], 0)
+// (s_e the sign product and m_e the minimum magnitude over the row's other edges, as
+// check_message, ldpc.rs:468-491), run for exactly T iterations, and its loss
+//   L = sum over the frame's n_full bits of softplus(-(1 - 2 c_v) post_v) / n_full
+// with the gradient of L with respect to every alpha and beta by reverse-mode
+// differentiation of the T unrolled iterations (the minimum is differentiated
+// through its argmin; sign and max(., 0) through their derivatives almost everywhere).
+// Weights are indexed [t][entry][r] (per lifted edge) or [t][entry] (shared across Z),
+// entry = the base-graph entry of the edge in table order, r its lifted row in the layer.
+struct Learned {
+  const Code* c;
+  int T;
+  bool shared;
+  std::vector<int> lstart;  // base row -> first entry
+  bool multi = false;       // loss of every iteration's output (weight 1/T each), else the last
+};
+
+static void learned_layers(const Code& c, std::vector<int>& lstart) {
+  const unsigned short(*table)[10] = c.bg == 1 ? NR_BG1 : NR_BG2;
+  int entries = c.bg == 1 ? NR_BG1_ENTRIES : NR_BG2_ENTRIES;
+  int rows_n = c.bg == 1 ? 46 : 42;
+  lstart.assign(rows_n + 1, 0);
+  for (int t = 0; t < entries; t++) lstart[table[t][0] + 1]++;
+  for (int i = 0; i < rows_n; i++) lstart[i + 1] += lstart[i];
+}
+
+static inline size_t widx(const Learned& L, int t, int entry, int r) {
+  int ne = L.lstart.back();
+  return L.shared ? (size_t)t * ne + entry : ((size_t)t * ne + entry) * L.c->z + r;
+}
+
+static double softplus(double x) { return x > 0 ? x + std::log1p(std::exp(-x)) : std::log1p(std::exp(x)); }
+static double sigmoid(double x) { return x >= 0 ? 1.0 / (1.0 + std::exp(-x)) : std::exp(x) / (1.0 + std::exp(x)); }
+
+// forward (and backward when ga != nullptr) of one frame; returns the loss
+static double learned_frame(const Learned& L, const double* full_llr, const uint8_t* cw, const double* alpha,
+                            const double* beta, double* post_out, double* ga, double* gb) {
+  const Code& c = *L.c;
+  const int z = c.z, rows_n = (int)L.lstart.size() - 1, T = L.T;
+  const int edges = c.start.back();
+  std::vector<double> post(full_llr, full_llr + c.n), c2v(edges, 0.0);
+  std::vector<double> X((size_t)T * edges), P;
+  if (L.multi) P.assign((size_t)T * c.n, 0.0);
+  for (int t = 0; t < T; t++) {
+    for (int Ly = 0; Ly < rows_n; Ly++)
+      for (int r = 0; r < z; r++) {
+        int row = Ly * z + r, d = (int)c.rows[row].size(), e0 = c.start[row];
+        double* x = &X[(size_t)t * edges + e0];
+        for (int i = 0; i < d; i++) x[i] = post[c.rows[row][i]] - c2v[e0 + i];
+        double sg = 1.0, m1 = INFINITY, m2 = INFINITY;
+        int i1 = 0;
+        for (int i = 0; i < d; i++) {
+          sg *= x[i] < 0 ? -1.0 : 1.0;
+          double a = std::fabs(x[i]);
+          if (a < m1) { m2 = m1; m1 = a; i1 = i; } else if (a < m2) m2 = a;
+        }
+        for (int i = 0; i < d; i++) {
+          double m = i == i1 ? m2 : m1, s = sg * (x[i] < 0 ? -1.0 : 1.0);
+          size_t w = widx(L, t, L.lstart[Ly] + i, r);
+          double a = alpha[w] * m - beta[w];
+          double y = s * (a > 0 ? a : 0.0);
+          c2v[e0 + i] = y;
+          post[c.rows[row][i]] = x[i] + y;
+        }
+      }
+    if (L.multi) std::copy(post.begin(), post.end(), P.begin() + (size_t)t * c.n);
+  }
+  auto bit_loss = [&](const double* p) {
+    double l = 0.0;
+    for (int v = 0; v < c.n; v++) l += softplus(-(1.0 - 2.0 * cw[v]) * p[v]);
+    return l / (double)c.n;
+  };
+  double loss = 0.0;
+  if (L.multi)
+    for (int t = 0; t < T; t++) loss += bit_loss(&P[(size_t)t * c.n]) / (double)T;
+  else
+    loss = bit_loss(post.data());
+  if (post_out) std::copy(post.begin(), post.end(), post_out);
+  if (!ga) return loss;
+  // reverse sweep
+  std::vector<double> gp(c.n, 0.0), gc(edges, 0.0);
+  auto add_loss_grad = [&](const double* p, double w) {
+    for (int v = 0; v < c.n; v++) {
+      double sgn = 1.0 - 2.0 * cw[v];
+      gp[v] += -sgn * sigmoid(-sgn * p[v]) * w / (double)c.n;
+    }
+  };
+  std::vector<double> gabs(32), gy(32);
+  for (int t = T - 1; t >= 0; t--) {
+    if (L.multi) add_loss_grad(&P[(size_t)t * c.n], 1.0 / (double)T);
+    else if (t == T - 1) add_loss_grad(post.data(), 1.0);
+    for (int Ly = rows_n - 1; Ly >= 0; Ly--)
+      for (int r = 0; r < z; r++) {
+        int row = Ly * z + r, d = (int)c.rows[row].size(), e0 = c.start[row];
+        const double* x = &X[(size_t)t * edges + e0];
+        double sg = 1.0, m1 = INFINITY, m2 = INFINITY;
+        int i1 = 0, i2 = 0;
+        for (int i = 0; i < d; i++) {
+          sg *= x[i] < 0 ? -1.0 : 1.0;
+          double a = std::fabs(x[i]);
+          if (a < m1) { m2 = m1; i2 = i1; m1 = a; i1 = i; } else if (a < m2) { m2 = a; i2 = i; }
+        }
+        if (d == 1) i2 = i1;
+        std::fill(gabs.begin(), gabs.begin() + d, 0.0);
+        for (int i = 0; i < d; i++) {
+          int v = c.rows[row][i];
+          double m = i == i1 ? m2 : m1, s = sg * (x[i] < 0 ? -1.0 : 1.0);
+          size_t w = widx(L, t, L.lstart[Ly] + i, r);
+          double a = alpha[w] * m - beta[w];
+          double g_y = gp[v] + gc[e0 + i];
+          double g_a = a > 0 ? g_y * s : 0.0;
+          ga[w] += g_a * m;
+          gb[w] -= g_a;
+          double g_m = g_a * alpha[w];
+          gabs[i == i1 ? i2 : i1] += g_m;
+        }
+        for (int i = 0; i < d; i++) {
+          int v = c.rows[row][i];
+          double g_x = gp[v] + (x[i] < 0 ? -1.0 : 1.0) * gabs[i];
+          gp[v] = g_x;
+          gc[e0 + i] = -g_x;
+        }
+      }
+  }
+  return loss;
+}
+
 }  // namespace oracle
 
 // ================================================================== C ABI (ctypes)
@@ -824,6 +955,30 @@ int or_bpsk_frame(void* h, uint64_t seed, uint64_t name_hash, uint64_t cond, uin
   result[0] = be;
   result[1] = (uint32_t)it;
   return 0;
+}
+
+// learned min-sum: forward (post_out n_full, optional) and gradients (ga/gb, optional,
+// accumulated) of `n` frames of e received LLRs and n_full codeword bits; returns the
+// mean loss over the frames
+double or_learned(void* h, int T, int shared, int multi, const double* alpha, const double* beta, const double* llr,
+                  const uint8_t* cw, int64_t n, double* post_out, double* ga, double* gb) {
+  Code* c = (Code*)h;
+  Learned L{c, T, shared != 0, {}, multi != 0};
+  learned_layers(*c, L.lstart);
+  std::vector<double> full(c->n);
+  double tot = 0.0;
+  for (int64_t f = 0; f < n; f++) {
+    full_llr<double>(*c, llr + f * c->e, full.data());
+    tot += learned_frame(L, full.data(), cw + f * c->n, alpha, beta, post_out ? post_out + f * c->n : nullptr, ga, gb);
+  }
+  return tot / (double)n;
+}
+
+int64_t or_learned_num_weights(void* h, int T, int shared) {
+  Code* c = (Code*)h;
+  std::vector<int> ls;
+  learned_layers(*c, ls);
+  return (int64_t)T * ls.back() * (shared ? 1 : c->z);
 }
 
 }  // extern "C"
