@@ -64,6 +64,18 @@ def test_f32_frames_draw_the_same_bits_and_close_llrs(cb, O):
     assert np.mean(np.sign(l32) == np.sign(l64)) > 0.9999
 
 
+@pytest.mark.parametrize("m", [64, 256])
+def test_f32_high_order_llrs_are_close_to_f64(cb, O, m):
+    spec = dict(k=1000, e=1512, m=m) if m == 64 else dict(k=1000, e=1504, m=m)
+    g32, _ = codes(cb, O, spec, "f32")
+    g64, _ = codes(cb, O, spec, "f64")
+    l32, i32 = g32.generate_frames(7, NAME, 0, 0, 8, 8.0, m)
+    l64, i64 = g64.generate_frames(7, NAME, 0, 0, 8, 8.0, m)
+    assert np.array_equal(i32, i64)
+    err = np.abs(l32.astype(np.float64) - l64) / np.maximum(np.abs(l64), 1.0)
+    assert np.median(err) < 1e-5 and np.mean(np.sign(l32) == np.sign(l64)) > 0.9999
+
+
 def test_f32_fer_is_statistically_the_f64_fer(cb, O):
     from conftest import load_package
 
