@@ -21,6 +21,7 @@ import os
 import numpy as np
 
 from .campaign import Grid, Stop, run  # noqa: F401
+from .mix import MIX_ITEM_DTYPE, MixBatch, autotune, draw_mixed_batch  # noqa: F401
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcomrs_gb300.so")
@@ -73,6 +74,13 @@ SYMBOLS = [
     ("cb_nms_gradients", _i32, [_vp, _vp, _vp, _i64, _i32, _vp, _vp, C.POINTER(_dbl)]),
     ("cb_nms_train_step", _i32, [_vp, _i32, _u64, _u64, _i64, _dbl, _dbl, _dbl, _i32, C.POINTER(_dbl)]),
     ("cb_nms_run_frames", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp]),
+    ("cb_mix_create", _i32, [_vp, _i64, _u64, _u64, _dbl, _i32, _i32, C.POINTER(_vp)]),
+    ("cb_mix_destroy", None, [_vp]),
+    ("cb_mix_last_error", C.c_char_p, [_vp]),
+    ("cb_mix_classes", _i32, [_vp, _i32, _vp, C.POINTER(_i32)]),
+    ("cb_mix_set_rows_per_thread", _i32, [_vp, _i32, _i32]),
+    ("cb_mix_run", _i32, [_vp, _u64, _vp]),
+    ("cb_mix_time_decode", _i32, [_vp, _i32, _i32, C.POINTER(_dbl)]),
     ("cb_decode_device_noalloc", _i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
     ("cb_xoshiro_jump", _i32, [_vp, _u64, _vp]),
 ]

@@ -12,6 +12,7 @@
 
 #include "../../include/comrs_gb300.h"
 #include "code_host.h"
+#include "dev_code.h"
 #include "kernels.h"
 
 #define CB_VERSION_STRING "comrs_gb300 0.1.0 (sm_103a)"
@@ -27,34 +28,6 @@ struct GenCache {
   double* d_points = nullptr;
   uint64_t* d_jumps = nullptr;
 };
-
-// Gray square QAM of order m, unit average energy (crates/com-mapping/src/
-// constellation.rs:168-202 with normalized, :396): natural row-major snake points,
-// label gray(i) for the i-th one, scaled by 1/sqrt(mean energy).
-bool qam_points(int m, std::vector<double>& pts, double& log_m) {
-  int side = (int)std::lround(std::sqrt((double)m));
-  if (m < 4 || (m & (m - 1)) || side * side != m || m > 256) return false;
-  std::vector<double> lv(side), nre, nim;
-  for (int i = 0; i < side; i++) lv[i] = 2.0 * (double)i - ((double)side - 1.0);
-  for (int r = 0; r < side; r++)
-    for (int t = 0; t < side; t++) {
-      int tt = (r % 2 == 1) ? side - 1 - t : t;
-      nre.push_back(lv[tt]);
-      nim.push_back(lv[side - 1 - r]);
-    }
-  pts.assign(2 * m, 0.0);
-  for (int i = 0; i < m; i++) {
-    int g = i ^ (i >> 1);
-    pts[2 * g] = nre[i];
-    pts[2 * g + 1] = nim[i];
-  }
-  double e = 0.0;
-  for (int i = 0; i < m; i++) e += pts[2 * i] * pts[2 * i] + pts[2 * i + 1] * pts[2 * i + 1];
-  double s = 1.0 / std::sqrt(e / (double)m);
-  for (double& v : pts) v *= s;
-  log_m = std::log((double)m);
-  return true;
-}
 
 }  // namespace
 
@@ -160,28 +133,14 @@ cb_status gen_config(cb_code* c, int m, GenCache** out) {
   auto it = c->gen.find(m);
   if (it != c->gen.end()) { *out = &it->second; return CB_OK; }
   GenCache g;
-  if (!qam_points(m, g.points, g.log_m)) return fail(c, CB_ERR_CONFIG, "modulation order must be 4, 16, 64 or 256");
+  if (!cbh::qam_points(m, g.points, g.log_m)) return fail(c, CB_ERR_CONFIG, "modulation order must be 4, 16, 64 or 256");
   g.m = m;
-  g.mbits = __builtin_ctz(m);
-  const int e = c->host.e, k = c->host.k_info, NT = cbk::kGenThreads;
-  g.n_pad = (g.mbits - e % g.mbits) % g.mbits;
-  int n_sym = (e + g.n_pad) / g.mbits;
-  g.bpc = (k + NT - 1) / NT;
-  g.spc = (n_sym + NT - 1) / NT;
-  std::vector<uint64_t> polys((size_t)(2 * NT + 1) * 4);
-  cbh::JumpPoly step_b = cbh::xoshiro_jump_poly((uint64_t)g.bpc), cur = cbh::xoshiro_jump_poly(0);
-  for (int t = 0; t < NT; t++) {
-    std::memcpy(&polys[(size_t)t * 4], cur.w, 32);
-    cur = cbh::xoshiro_jump_mul(cur, step_b);
-  }
-  cbh::JumpPoly step_s = cbh::xoshiro_jump_poly(2ull * g.spc);
-  cur = cbh::xoshiro_jump_poly((uint64_t)k + g.n_pad);
-  for (int t = 0; t < NT; t++) {
-    std::memcpy(&polys[(size_t)(NT + t) * 4], cur.w, 32);
-    cur = cbh::xoshiro_jump_mul(cur, step_s);
-  }
-  cbh::JumpPoly padp = cbh::xoshiro_jump_poly((uint64_t)k);
-  std::memcpy(&polys[(size_t)(2 * NT) * 4], padp.w, 32);
+  const cbh::GenTables t = cbh::gen_tables(c->host.k_info, c->host.e, m, cbk::kGenThreads);
+  g.mbits = t.mbits;
+  g.n_pad = t.n_pad;
+  g.bpc = t.bits_per_chunk;
+  g.spc = t.syms_per_chunk;
+  const std::vector<uint64_t>& polys = t.jumps;
   CB_CUDA(c, cudaMalloc(&g.d_points, sizeof(double) * 2 * m));
   CB_CUDA(c, cudaMemcpy(g.d_points, g.points.data(), sizeof(double) * 2 * m, cudaMemcpyHostToDevice));
   CB_CUDA(c, cudaMalloc(&g.d_jumps, polys.size() * 8));
@@ -386,12 +345,9 @@ cb_status cb_code_create(const cb_code_desc* d, cb_code** out) {
     return fail(nullptr, CB_ERR_CONFIG, err);
   }
   // the decoder is compiled for the row degrees of the NR base graphs
-  for (int L = 0; L < c->host.rows_n; L++) {
-    int deg = c->host.layer_start[L + 1] - c->host.layer_start[L];
-    if (!((deg >= 3 && deg <= 10) || deg == 19)) {
-      delete c;
-      return fail(nullptr, CB_ERR_CONFIG, "a base-graph row degree outside 3..10 and 19");
-    }
+  if (!cbk::degrees_supported(c->host)) {
+    delete c;
+    return fail(nullptr, CB_ERR_CONFIG, "a base-graph row degree outside 3..10 and 19");
   }
   c->device = d->device;
   c->precision = d->precision;
@@ -399,28 +355,7 @@ cb_status cb_code_create(const cb_code_desc* d, cb_code** out) {
   c->cfg.alpha = d->alpha;
   c->cfg.layered = d->layered;
   c->cfg.max_iterations = d->max_iterations;
-  const cbh::NrCode& h = c->host;
-  cbd::DevCode& v = c->dev;
-  std::memset(&v, 0, sizeof v);
-  v.bg = h.bg;
-  v.z = h.z;
-  v.cols_k = h.cols_k;
-  v.rows_n = h.rows_n;
-  v.n_full = h.n_full;
-  v.k = h.k;
-  v.k_info = h.k_info;
-  v.e = h.e;
-  v.qm = h.qm;
-  v.max_degree = h.max_degree;
-  v.n_entries = (int)h.entry_col.size();
-  v.n_core_terms = (int)h.core_terms.size();
-  v.map_is_offset = h.map_is_offset;
-  v.has_repeats = h.has_repeats;
-  for (int i = 0; i <= h.rows_n; i++) v.layer_start[i] = (uint16_t)h.layer_start[i];
-  for (int t = 0; t < v.n_entries; t++) v.entry[t] = ((uint32_t)h.entry_col[t] << 16) | h.entry_shift[t];
-  for (int t = 0; t < v.n_core_terms; t++)
-    v.core_term[t] = ((uint32_t)h.core_terms[t].block << 20) | ((uint32_t)h.core_terms[t].src << 16) |
-                     h.core_terms[t].shift;
+  cbk::fill_dev_code(c->host, c->dev);
   *out = c;
   return CB_OK;
 }

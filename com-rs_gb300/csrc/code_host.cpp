@@ -2,6 +2,7 @@
 #include "code_host.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "nr_base_graphs.inc"
@@ -254,6 +255,55 @@ void xoshiro_apply_jump(uint64_t s[4], const JumpPoly& p) {
     xoshiro_step(s);
   }
   std::memcpy(s, acc, sizeof acc);
+}
+
+bool qam_points(int m, std::vector<double>& pts, double& log_m) {
+  int side = (int)std::lround(std::sqrt((double)m));
+  if (m < 4 || (m & (m - 1)) || side * side != m || m > 256) return false;
+  std::vector<double> lv(side), nre, nim;
+  for (int i = 0; i < side; i++) lv[i] = 2.0 * (double)i - ((double)side - 1.0);
+  for (int r = 0; r < side; r++)
+    for (int t = 0; t < side; t++) {
+      int tt = (r % 2 == 1) ? side - 1 - t : t;
+      nre.push_back(lv[tt]);
+      nim.push_back(lv[side - 1 - r]);
+    }
+  pts.assign(2 * m, 0.0);
+  for (int i = 0; i < m; i++) {
+    int g = i ^ (i >> 1);
+    pts[2 * g] = nre[i];
+    pts[2 * g + 1] = nim[i];
+  }
+  double e = 0.0;
+  for (int i = 0; i < m; i++) e += pts[2 * i] * pts[2 * i] + pts[2 * i + 1] * pts[2 * i + 1];
+  double s = 1.0 / std::sqrt(e / (double)m);
+  for (double& v : pts) v *= s;
+  log_m = std::log((double)m);
+  return true;
+}
+
+GenTables gen_tables(int k_info, int e, int m, int threads) {
+  GenTables g;
+  g.mbits = __builtin_ctz(m);
+  g.n_pad = (g.mbits - e % g.mbits) % g.mbits;
+  int n_sym = (e + g.n_pad) / g.mbits;
+  g.bits_per_chunk = (k_info + threads - 1) / threads;
+  g.syms_per_chunk = (n_sym + threads - 1) / threads;
+  g.jumps.assign((size_t)(2 * threads + 1) * 4, 0);
+  JumpPoly step_b = xoshiro_jump_poly((uint64_t)g.bits_per_chunk), cur = xoshiro_jump_poly(0);
+  for (int t = 0; t < threads; t++) {
+    std::memcpy(&g.jumps[(size_t)t * 4], cur.w, 32);
+    cur = xoshiro_jump_mul(cur, step_b);
+  }
+  JumpPoly step_s = xoshiro_jump_poly(2ull * g.syms_per_chunk);
+  cur = xoshiro_jump_poly((uint64_t)k_info + g.n_pad);
+  for (int t = 0; t < threads; t++) {
+    std::memcpy(&g.jumps[(size_t)(threads + t) * 4], cur.w, 32);
+    cur = xoshiro_jump_mul(cur, step_s);
+  }
+  JumpPoly padp = xoshiro_jump_poly((uint64_t)k_info);
+  std::memcpy(&g.jumps[(size_t)(2 * threads) * 4], padp.w, 32);
+  return g;
 }
 
 }  // namespace cbh

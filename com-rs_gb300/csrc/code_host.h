@@ -64,4 +64,17 @@ JumpPoly xoshiro_jump_mul(const JumpPoly& a, const JumpPoly& b);
 // applies a jump polynomial to a state (host copy of the device routine, for tests)
 void xoshiro_apply_jump(uint64_t s[4], const JumpPoly& p);
 
+// Gray square QAM of order m, unit average energy: 2m doubles (re, im) by label, and
+// ln m (crates/com-mapping/src/constellation.rs:168-202, :396; demapper.rs:279)
+bool qam_points(int m, std::vector<double>& pts, double& log_m);
+
+// The frame generator's chunking of one frame's draws over `threads` threads and the
+// jump polynomials of the chunk starts: [threads] info-bit chunks, [threads] symbol
+// chunks, then the padding bits (4 words each).
+struct GenTables {
+  int mbits = 0, n_pad = 0, bits_per_chunk = 0, syms_per_chunk = 0;
+  std::vector<uint64_t> jumps;
+};
+GenTables gen_tables(int k_info, int e, int m, int threads);
+
 }  // namespace cbh

@@ -5,6 +5,8 @@
 
 #include <cstdint>
 
+#include "device_common.cuh"
+
 namespace cbk {
 namespace {
 
@@ -110,6 +112,209 @@ __device__ __forceinline__ bool some_check_fails(const T* post, uint32_t* hd, co
   }
   return __syncthreads_or(bad) != 0;
 }
+
+// One lifted row of a layer: thread r, degree D known at compile time.
+// old state (a1, a2, mt) -> new state (n1, n2, nm); post updated in place.
+template <typename T, int D>
+__device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t* __restrict__ ent, int r, int z,
+                                           T a1, T a2, uint32_t mt, int rule, T alpha, T& n1, T& n2,
+                                           uint32_t& nm) {
+  int off[D];
+  T x[D];
+  const int old_i1 = (int)(mt & 31u);
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    const uint32_t en = ent[e];
+    // (r + shift) mod Z with one unsigned min: r + shift < 2Z
+    unsigned c = (unsigned)r + (en & 0xffffu);
+    unsigned cm = c - (unsigned)z;
+    off[e] = (int)(en >> 16) * z + (int)min(c, cm);
+    T mag = (e == old_i1) ? a2 : a1;
+    T old = ((mt >> (8 + e)) & 1u) ? -mag : mag;
+    x[e] = sub_rn(post[off[e]], old);
+  }
+  // check_message, min-sum branch (ldpc.rs:468-491): sign product with `l < 0`, strict
+  // `<` for the minimum and its index, min(m2, a) for the second (equal for non-NaN,
+  // and a NaN is skipped by both)
+  uint32_t par = (uint32_t)(x[0] < (T)0);
+  T m1 = fmin(fabs(x[0]), infinity<T>()), m2 = infinity<T>();
+  int i1 = 0;
+#pragma unroll
+  for (int e = 1; e < D; e++) {
+    par ^= (uint32_t)(x[e] < (T)0);
+    T av = fabs(x[e]);
+    bool lt = av < m1;
+    m2 = lt ? m1 : fmin(m2, av);
+    m1 = lt ? av : m1;
+    i1 = lt ? e : i1;
+  }
+  if (rule == cbd::RULE_NMS) {
+    n1 = mul_rn(alpha, m1);
+    n2 = mul_rn(alpha, m2);
+  } else {
+    n1 = fmax(sub_rn(m1, alpha), (T)0);
+    n2 = fmax(sub_rn(m2, alpha), (T)0);
+  }
+  nm = (uint32_t)i1;
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    uint32_t ng = par ^ (uint32_t)(x[e] < (T)0);
+    T mag = (e == i1) ? n2 : n1;
+    T o = ng ? -mag : mag;
+    post[off[e]] = add_rn(x[e], o);
+    nm |= ng << (8 + e);
+  }
+}
+
+// f32 row update with fewer integer-pipe operations (same results as row_update for
+// finite LLRs):
+//   * min and second min with min/max only; the edges that receive the second minimum
+//     are those whose magnitude equals the minimum (if several do, the two minima are
+//     equal, so every edge gets the same magnitude, as in the reference);
+//   * the sign test `x < 0` is the sign bit of x: the posteriors never hold -0.0 (they
+//     start as 0.0 + LLR or 30.0, and a difference or sum is -0.0 only when an operand
+//     already is), so no message input x = post - c2v is -0.0 either;
+//   * outgoing signs are applied and collected with bit operations.
+// State word: bits 0-4 an edge holding the second minimum, bits 8.. the outgoing sign of
+// edge e at bit 8 + (D - 1 - e).
+template <int D>
+__device__ __forceinline__ void row_update_lean(float* __restrict__ post, const uint32_t* __restrict__ ent, int r,
+                                                int z, float a1, float a2, uint32_t mt, int rule, float alpha,
+                                                float& n1, float& n2, uint32_t& nm) {
+  int off[D];
+  float x[D];
+  const int old_i1 = (int)(mt & 31u);
+  const uint32_t t0 = mt << (24 - D);  // the old sign of edge 0 at bit 31
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    const uint32_t en = ent[e];
+    unsigned c = (unsigned)r + (en & 0xffffu);
+    unsigned cm = c - (unsigned)z;
+    off[e] = (int)(en >> 16) * z + (int)min(c, cm);
+    float mag = (e == old_i1) ? a2 : a1;
+    uint32_t ob = __float_as_uint(mag) | ((t0 << e) & 0x80000000u);
+    x[e] = __fsub_rn(post[off[e]], __uint_as_float(ob));
+  }
+  uint32_t par = 0;
+  float m1 = infinity<float>(), m2 = infinity<float>();
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    par ^= __float_as_uint(x[e]);
+    float av = fabsf(x[e]);
+    m2 = fminf(m2, fmaxf(m1, av));
+    m1 = fminf(m1, av);
+  }
+  if (rule == cbd::RULE_NMS) {
+    n1 = __fmul_rn(alpha, m1);
+    n2 = __fmul_rn(alpha, m2);
+  } else {
+    n1 = fmaxf(__fsub_rn(m1, alpha), 0.0f);
+    n2 = fmaxf(__fsub_rn(m2, alpha), 0.0f);
+  }
+  const uint32_t ps = par & 0x80000000u;
+  const uint32_t n1p = __float_as_uint(n1) | ps, n2p = __float_as_uint(n2) | ps;
+  uint32_t sm = 0;
+  int i1 = 0;
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    bool eq = fabsf(x[e]) == m1;
+    uint32_t magp = eq ? n2p : n1p;
+    i1 = eq ? e : i1;
+    uint32_t ob = magp ^ (__float_as_uint(x[e]) & 0x80000000u);
+    post[off[e]] = __fadd_rn(x[e], __uint_as_float(ob));
+    sm = (sm << 1) | (ob >> 31);
+  }
+  nm = (sm << 8) | (uint32_t)i1;
+}
+
+template <typename T>
+__device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent, int r, int z, T a1, T a2,
+                                             uint32_t mt, int rule, T alpha, T& n1, T& n2, uint32_t& nm) {
+#ifndef CB_F32_CLASSIC_ROWS
+  if constexpr (sizeof(T) == 4) {
+    switch (d) {
+      case 3: row_update_lean<3>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 4: row_update_lean<4>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 5: row_update_lean<5>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 6: row_update_lean<6>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 7: row_update_lean<7>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 8: row_update_lean<8>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 9: row_update_lean<9>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      case 10: row_update_lean<10>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+      default: row_update_lean<19>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    }
+    return;
+  }
+#endif
+  switch (d) {
+    case 3: row_update<T, 3>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 4: row_update<T, 4>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 5: row_update<T, 5>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 6: row_update<T, 6>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 7: row_update<T, 7>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 8: row_update<T, 8>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 9: row_update<T, 9>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 10: row_update<T, 10>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    default: row_update<T, 19>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+  }
+}
+
+// check-node state of one lifted row: f32 as one 16-byte record {n1, n2, meta, 0};
+// f64 as a 16-byte {n1, n2} record plus a separate plane of meta words
+template <typename T>
+struct StateSlot;
+// The state records of all resident CTAs (86 MB at BG1 Z = 384) fit in L2, but the LLR
+// stream of a launch (830 MB for 8192 codewords) would evict them: the records are read
+// and written with an L2 evict-last policy, the LLRs with streaming loads.
+__device__ __forceinline__ uint64_t l2_evict_last_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+template <>
+struct StateSlot<float> {
+  uint4* rec;
+  uint64_t pol;
+  __device__ __forceinline__ StateSlot(unsigned char* base, int rows)
+      : rec(reinterpret_cast<uint4*>(base)), pol(l2_evict_last_policy()) {
+    (void)rows;
+  }
+  __device__ __forceinline__ void load(int row, float& a1, float& a2, uint32_t& mt) const {
+    uint32_t x, y, zz, w;
+    asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(x), "=r"(y), "=r"(zz), "=r"(w)
+                 : "l"(rec + row), "l"(pol));
+    (void)w;
+    a1 = __uint_as_float(x);
+    a2 = __uint_as_float(y);
+    mt = zz;
+  }
+  __device__ __forceinline__ void store(int row, float n1, float n2, uint32_t nm) const {
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(rec + row),
+                 "r"(__float_as_uint(n1)), "r"(__float_as_uint(n2)), "r"(nm), "r"(0u), "l"(pol)
+                 : "memory");
+  }
+  static __host__ __device__ size_t bytes(int rows) { return (size_t)rows * 16; }
+};
+template <>
+struct StateSlot<double> {
+  double2* rec;
+  uint32_t* meta;
+  __device__ __forceinline__ StateSlot(unsigned char* base, int rows)
+      : rec(reinterpret_cast<double2*>(base)), meta(reinterpret_cast<uint32_t*>(base + (size_t)rows * 16)) {}
+  __device__ __forceinline__ void load(int row, double& a1, double& a2, uint32_t& mt) const {
+    double2 v = rec[row];
+    a1 = v.x;
+    a2 = v.y;
+    mt = meta[row];
+  }
+  __device__ __forceinline__ void store(int row, double n1, double n2, uint32_t nm) const {
+    rec[row] = make_double2(n1, n2);
+    meta[row] = nm;
+  }
+  static __host__ __device__ size_t bytes(int rows) { return (size_t)rows * 20; }
+};
 
 }  // namespace
 }  // namespace cbk

@@ -41,10 +41,9 @@ constexpr int NT = kGenThreads;
 
 __device__ __forceinline__ int gray(int i) { return i ^ (i >> 1); }
 
+// One frame by one CTA of NT threads: code `c`, frame parameters `a`.
 template <typename T>
-__global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const cbd::DevCode& c = a.code;
+__device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>& a, unsigned char* smem) {
   const int z = c.z, tid = threadIdx.x;
   const int n_sym = (c.e + a.n_pad) / a.mbits;
   // shared layout: points (2M doubles) | syndromes (4Z) | codeword (n_full) | labels
@@ -55,9 +54,7 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
   uint8_t* pad = lab + n_sym;  // padding bits (< mbits)
   __shared__ double s_sigma2;
   __shared__ unsigned int s_hist[256];
-  const long long frame = (long long)blockIdx.x;
-  if (frame >= a.n_frames) return;
-  const uint64_t fidx = a.first_frame + (uint64_t)frame;
+  const uint64_t fidx = a.frame_index;
 
   for (int i = tid; i < 2 * a.m; i += NT) pts[i] = a.points[i];
   // ---- info bits: chunk [tid * bpc, (tid + 1) * bpc)
@@ -82,7 +79,7 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
     for (int b0 = warp * 32; b0 < c.k_info; b0 += (NT / 32) * 32) {
       int v = b0 + lane;
       uint32_t word = __ballot_sync(0xffffffffu, v < c.k_info && cw[v]);
-      if (lane == 0) a.info_out[(size_t)frame * wpf + (b0 >> 5)] = word;
+      if (lane == 0) a.info_out[b0 >> 5] = word;
     }
   }
   // ---- encoder: core syndromes over the systematic columns
@@ -135,7 +132,7 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
     for (int b0 = warp * 32; b0 < c.n_full; b0 += (NT / 32) * 32) {
       int v = b0 + lane;
       uint32_t word = __ballot_sync(0xffffffffu, v < c.n_full && cw[v]);
-      if (lane == 0) a.cw_out[(size_t)frame * wpc + (b0 >> 5)] = word;
+      if (lane == 0) a.cw_out[b0 >> 5] = word;
     }
   }
   // ---- labels, MSB first (bits_to_index, com-math bits.rs:68-70)
@@ -159,8 +156,7 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
         e = __dadd_rn(e, __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
       }
       double p = __ddiv_rn(__dadd_rn(0.0, e), (double)n_sym);
-      double be = a.ebn0_frames ? a.b_bits * pow(10.0, (double)a.ebn0_frames[frame] / 10.0) : a.b_ebn0;
-      s_sigma2 = __ddiv_rn(p, be);
+      s_sigma2 = __ddiv_rn(p, a.b_ebn0);
     }
   } else {
     // f32 frames: the label histogram, then the sum over the M labels
@@ -174,8 +170,7 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
         float re = (float)pts[2 * i], im = (float)pts[2 * i + 1];
         e += (float)s_hist[i] * (re * re + im * im);
       }
-      float be = a.ebn0_frames ? (float)a.b_bits * exp10f(a.ebn0_frames[frame] / 10.0f) : (float)a.b_ebn0;
-      s_sigma2 = (double)(e / (float)n_sym / be);
+      s_sigma2 = (double)(e / (float)n_sym / (float)a.b_ebn0);
     }
   }
   __syncthreads();
@@ -185,7 +180,7 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
   if (s0 >= s1) return;
   cbd::Xoshiro r = cbd::stream(a.seed, a.name_hash, a.cond, fidx);
   cbd::xoshiro_jump(r, a.jumps + 4 * (NT + tid));
-  T* out = a.llr_out + (size_t)frame * c.e;
+  T* out = a.llr_out;
   if (sizeof(T) == 8) {
     const double sd = __dsqrt_rn(sigma2);
     const double uniform = -a.log_m;
@@ -259,6 +254,63 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
   }
 }
 
+
+template <typename T>
+__global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const long long frame = (long long)blockIdx.x;
+  if (frame >= a.n_frames) return;
+  const cbd::DevCode& c = a.code;
+  GenFrame<T> g;
+  g.m = a.m;
+  g.mbits = a.mbits;
+  g.n_pad = a.n_pad;
+  g.bits_per_chunk = a.bits_per_chunk;
+  g.syms_per_chunk = a.syms_per_chunk;
+  g.points = a.points;
+  g.log_m = a.log_m;
+  if (!a.ebn0_frames) g.b_ebn0 = a.b_ebn0;
+  else if (sizeof(T) == 8) g.b_ebn0 = a.b_bits * pow(10.0, (double)a.ebn0_frames[frame] / 10.0);
+  else g.b_ebn0 = (double)((float)a.b_bits * exp10f(a.ebn0_frames[frame] / 10.0f));
+  g.jumps = a.jumps;
+  g.seed = a.seed;
+  g.name_hash = a.name_hash;
+  g.cond = a.cond;
+  g.frame_index = a.first_frame + (uint64_t)frame;
+  g.llr_out = a.llr_out + (size_t)frame * c.e;
+  g.info_out = a.info_out + (size_t)frame * ((c.k_info + 31) >> 5);
+  g.cw_out = a.cw_out ? a.cw_out + (size_t)frame * ((c.n_full + 31) >> 5) : nullptr;
+  gen_one<T>(c, g, smem);
+}
+
+// The frames of a mixed batch: CTA i generates item i of the batch (its own code,
+// modulation, Eb/N0 and stream position) into the batch's LLR and info buffers.
+__global__ void __launch_bounds__(NT) gen_mix_kernel(const __grid_constant__ GenMixArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const long long i = (long long)blockIdx.x;
+  if (i >= a.n_items) return;
+  const MixItem it = a.items[i];
+  const GenConfig gc = a.configs[it.config];
+  const cbd::DevCode& c = a.codes[it.code];
+  GenFrame<float> g;
+  g.m = gc.m;
+  g.mbits = gc.mbits;
+  g.n_pad = gc.n_pad;
+  g.bits_per_chunk = gc.bits_per_chunk;
+  g.syms_per_chunk = gc.syms_per_chunk;
+  g.points = gc.points;
+  g.log_m = gc.log_m;
+  g.b_ebn0 = it.b_ebn0;
+  g.jumps = gc.jumps;
+  g.seed = a.seed;
+  g.name_hash = a.name_hash;
+  g.cond = it.cond;
+  g.frame_index = it.frame + (a.epoch ? *a.epoch * a.epoch_stride : 0ull);
+  g.llr_out = a.llr + it.llr_offset;
+  g.info_out = a.info + it.info_offset;
+  g.cw_out = nullptr;
+  gen_one<float>(c, g, smem);
+}
 }  // namespace
 
 size_t gen_smem_bytes(const cbd::DevCode& c, int m, int mbits, int n_pad) {
@@ -278,5 +330,13 @@ cudaError_t launch_gen(const GenArgs<T>& a, cudaStream_t stream) {
 
 template cudaError_t launch_gen<double>(const GenArgs<double>&, cudaStream_t);
 template cudaError_t launch_gen<float>(const GenArgs<float>&, cudaStream_t);
+
+cudaError_t launch_gen_mix(const GenMixArgs& a, size_t smem, cudaStream_t stream) {
+  void* k = (void*)gen_mix_kernel;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {(void*)&a};
+  return cudaLaunchKernel(k, dim3((unsigned)a.n_items), dim3(NT), args, smem, stream);
+}
 
 }  // namespace cbk

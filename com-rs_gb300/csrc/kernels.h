@@ -55,6 +55,75 @@ struct GenArgs {
 };
 constexpr int kGenThreads = 128;
 
+// The generation parameters of one frame (everything but the code).
+template <typename T>
+struct GenFrame {
+  int32_t m, mbits, n_pad, bits_per_chunk, syms_per_chunk;
+  const double* points;
+  double log_m, b_ebn0;
+  const uint64_t* jumps;
+  uint64_t seed, name_hash, cond, frame_index;
+  T* llr_out;          // this frame's E LLRs
+  uint32_t* info_out;  // its packed info bits
+  uint32_t* cw_out;    // its packed codeword (optional)
+};
+
+// ---- mixed batches (mix.cu, gen.cu): codewords of different codes in one launch
+// per (code, modulation) pair: the generator's tables
+struct GenConfig {
+  int32_t m, mbits, n_pad, bits_per_chunk, syms_per_chunk;
+  const double* points;
+  double log_m;
+  const uint64_t* jumps;
+};
+// one codeword of a mixed batch
+struct MixItem {
+  int32_t code;         // index into the batch's codes
+  int32_t config;       // index into the batch's generator configs
+  uint64_t cond, frame; // its stream position: stream(seed, name, cond, frame)
+  double b_ebn0;        // (log2 M * R) * db2lin(Eb/N0), computed on the host
+  int64_t llr_offset;   // its LLRs in the batch buffer (elements)
+  int64_t info_offset;  // its packed info bits (words)
+  int32_t index;        // its position in the caller's order (the result slot)
+  int32_t reserved;
+};
+struct GenMixArgs {
+  const cbd::DevCode* codes;
+  const GenConfig* configs;
+  const MixItem* items;
+  int64_t n_items;
+  uint64_t seed, name_hash;
+  const uint64_t* epoch;   // optional: frames advance by epoch * epoch_stride per replay
+  uint64_t epoch_stride;
+  float* llr;
+  uint32_t* info;
+};
+cudaError_t launch_gen_mix(const GenMixArgs& a, size_t smem, cudaStream_t stream);
+
+// a lifting-size class of a mixed batch and its slot layout in a 384-thread CTA
+struct MixClass {
+  int32_t z, slot_threads, slots, rows_per_thread;
+  int64_t first, count;  // its items in the sorted batch
+  int32_t smem_per_slot, state_per_slot, max_ncol, reserved;
+};
+struct MixDecodeArgs {
+  const cbd::DevCode* codes;
+  const MixItem* items;     // sorted by class
+  const MixClass* classes;
+  int32_t n_classes, rule, max_it;
+  float alpha;
+  const float* llr;
+  const uint32_t* info;
+  cbd::FrameResult* results;  // by MixItem::index
+  unsigned long long* counters;  // one queue per class
+  unsigned char* state;
+  size_t state_per_cta;
+};
+size_t mix_slot_smem_bytes(int z);
+int mix_decode_grid(size_t smem, int device);
+cudaError_t launch_mix_decode(const MixDecodeArgs& a, int grid, size_t smem, cudaStream_t stream);
+size_t gen_smem_bytes(const cbd::DevCode& c, int m, int mbits, int n_pad);
+
 // Learned min-sum (nms_learned.cu): forward (training or evaluation) and backward.
 struct LearnedArgs {
   cbd::DevCode code;

@@ -166,6 +166,38 @@ cb_status cb_nms_run_frames(cb_nms* nms, int32_t modulation_order, uint64_t seed
                             uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,
                             cb_frame_result* out);
 
+/* ---- Mixed batches: codewords of different base graphs, lifting sizes, rates,
+ * modulations and Eb/N0 generated and decoded together.  The batch's codewords are
+ * sorted by lifting size into classes; one persistent kernel decodes every class,
+ * each CTA split into slots that take codewords from the class's queue one after
+ * another (per-codeword early exit, work stealing).  Generator and decoder are
+ * captured once as a CUDA graph and replayed by cb_mix_run.  Every record equals
+ * cb_run_frames of the item's own code on the same stream position. */
+typedef struct {
+  int32_t base_graph;       /* 1 or 2 */
+  int32_t lifting_size;     /* Z */
+  int32_t k_info, e;        /* K' and E; the rate matching must be the plain 2Z + t */
+  int32_t modulation_order; /* 4, 16, 64, 256 */
+  int32_t reserved;
+  double ebn0_db;
+  uint64_t condition, frame; /* stream(seed, name, condition, frame + epoch * n_items) */
+} cb_mix_item;
+typedef struct cb_mix cb_mix;
+cb_status cb_mix_create(const cb_mix_item* items, int64_t n_items, uint64_t seed, uint64_t name_hash, double alpha,
+                        int32_t max_iterations, int32_t device, cb_mix** out);
+void cb_mix_destroy(cb_mix* mix);
+const char* cb_mix_last_error(const cb_mix* mix);
+/* per class (up to `capacity`), 8 values: Z, codewords, rows per thread, slots per
+ * CTA, threads per slot, shared bytes per slot, resident CTAs, first sorted item */
+cb_status cb_mix_classes(const cb_mix* mix, int32_t capacity, int64_t* info, int32_t* n_classes);
+/* the autotuner's knob: lifted rows per thread (1, 2 or 4) of one class */
+cb_status cb_mix_set_rows_per_thread(cb_mix* mix, int32_t class_index, int32_t rows_per_thread);
+/* generate and decode the batch at `epoch` (replays the graph); records in the items'
+ * order into `out` (host, n_items records; NULL to skip the copy) */
+cb_status cb_mix_run(cb_mix* mix, uint64_t epoch, cb_frame_result* out);
+/* the best of `reps` event-timed decode phases of one class (-1: all classes) */
+cb_status cb_mix_time_decode(cb_mix* mix, int32_t class_index, int32_t reps, double* ms);
+
 /* cb_decode_device for callers that cannot allocate device memory (a host framework
  * that owns all device memory through its own pool, or a real-time loop that forbids
  * cudaMalloc after start-up).  No counterpart in the reference: it is an addition of
