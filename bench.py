@@ -264,6 +264,31 @@ def run_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def run_profile_case(args):
+    """The small case the committed ncu summaries capture: `frames` C2 codewords generated
+    once (Eb/N0 = 1 dB), then decoded three times."""
+    import torch
+
+    cb = importlib.import_module("com-rs_gb300")
+    L = cb.lib()
+    n = args.frames
+    code = cb.NrLdpc(K_INFO, E, base_graph=BG, lifting_size=Z, precision="f32")
+    llr = torch.empty((n, E), dtype=torch.float32, device="cuda")
+    info = torch.empty((n, (K_INFO + 31) // 32), dtype=torch.int32, device="cuda")
+    bits = torch.empty((n, (K_INFO + 31) // 32), dtype=torch.int32, device="cuda")
+    iters = torch.empty(n, dtype=torch.int32, device="cuda")
+    sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    st = L.cb_generate_frames_device(code._h, M, SEED, cb.fnv1a64(NAME), 0, 0, n, 1.0, C.c_void_p(llr.data_ptr()),
+                                     C.c_void_p(info.data_ptr()), sp)
+    for _ in range(3):
+        st |= L.cb_decode_device(code._h, C.c_void_p(llr.data_ptr()), n, C.c_void_p(bits.data_ptr()), None,
+                                 C.c_void_p(iters.data_ptr()), sp)
+    torch.cuda.synchronize()
+    if st:
+        raise cb.ComrsError(st, L.cb_last_error(code._h).decode())
+    print(json.dumps({"profile_case": n, "mean_iterations": float(iters.float().mean())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -272,7 +297,12 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--frames", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="generate --frames C2 codewords and decode them three times (for ncu)")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
