@@ -121,7 +121,11 @@ __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(co
             const int d = c.layer_start[L + 1] - s0;
             T n1, n2;
             uint32_t nm;
-            row_dispatch<T>(d, post, c.entry + s0, tid, z, a1, a2, mt, rule, alpha, n1, n2, nm);
+            if constexpr (sizeof(T) == 4)
+              row_dispatch_lean(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z}, a1, a2, mt, rule, alpha,
+                                n1, n2, nm);
+            else
+              row_dispatch<T>(d, post, c.entry + s0, tid, z, a1, a2, mt, rule, alpha, n1, n2, nm);
             st.store(L * z + tid, n1, n2, nm);
           }
           a1 = p1;

@@ -166,44 +166,93 @@ __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t*
   }
 }
 
+// Byte offset in post of edge e's variable for lifted row r, from the packed entry
+// (base column << 16 | shift).
+struct EdgeAddrPacked {
+  const uint32_t* ent;
+  int r, z;
+  __device__ __forceinline__ int operator()(int e) const {
+    const uint32_t en = ent[e];
+    unsigned c = (unsigned)r + (en & 0xffffu);
+    unsigned cm = c - (unsigned)z;
+    return 4 * ((int)(en >> 16) * z + (int)min(c, cm));
+  }
+};
+// The same from the per-entry table {4 (col Z + shift), Z - shift} of DevCode::eaddr:
+// 4 (col Z + (r + shift) mod Z) = 4 r + x, less 4 Z when r >= Z - shift.
+struct EdgeAddrTable {
+  const uint2* tab;
+  int r, r4, z4;
+  __device__ __forceinline__ int operator()(int e) const {
+    const uint2 t = tab[e];
+    const int o = r4 + (int)t.x;
+    return r >= (int)t.y ? o - z4 : o;
+  }
+};
+
+__device__ __forceinline__ float ld_post(const float* post, int off) {
+  return *reinterpret_cast<const float*>(reinterpret_cast<const char*>(post) + off);
+}
+__device__ __forceinline__ void st_post(float* post, int off, float v) {
+  *reinterpret_cast<float*>(reinterpret_cast<char*>(post) + off) = v;
+}
+// |d| = min(|a|, |b|), sign(d) = sign(a) xor sign(b)
+__device__ __forceinline__ float min_xorsign_abs(float a, float b) {
+  float d;
+  asm("min.xorsign.abs.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+  return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
 // f32 row update with fewer integer-pipe operations (same results as row_update for
 // finite LLRs):
-//   * min and second min with min/max only; the edges that receive the second minimum
-//     are those whose magnitude equals the minimum (if several do, the two minima are
-//     equal, so every edge gets the same magnitude, as in the reference);
+//   * the edge addresses come from a functor (packed entries, or the per-entry table);
+//   * the minimum and second minimum are taken two edges at a time with min/max only
+//     (min.xorsign.abs and the three-input min), and the minimum's sign bit collects
+//     the sign product; the edges that receive the second minimum are those whose
+//     magnitude equals the minimum (if several do, the two minima are equal, so every
+//     edge gets the same magnitude, as in the reference);
 //   * the sign test `x < 0` is the sign bit of x: the posteriors never hold -0.0 (they
 //     start as 0.0 + LLR or 30.0, and a difference or sum is -0.0 only when an operand
 //     already is), so no message input x = post - c2v is -0.0 either;
 //   * outgoing signs are applied and collected with bit operations.
 // State word: bits 0-4 an edge holding the second minimum, bits 8.. the outgoing sign of
 // edge e at bit 8 + (D - 1 - e).
-template <int D>
-__device__ __forceinline__ void row_update_lean(float* __restrict__ post, const uint32_t* __restrict__ ent, int r,
-                                                int z, float a1, float a2, uint32_t mt, int rule, float alpha,
-                                                float& n1, float& n2, uint32_t& nm) {
+template <int D, typename Addr>
+__device__ __forceinline__ void row_update_lean(float* __restrict__ post, const Addr& addr, float a1, float a2,
+                                                uint32_t mt, int rule, float alpha, float& n1, float& n2,
+                                                uint32_t& nm) {
   int off[D];
   float x[D];
   const int old_i1 = (int)(mt & 31u);
   const uint32_t t0 = mt << (24 - D);  // the old sign of edge 0 at bit 31
 #pragma unroll
   for (int e = 0; e < D; e++) {
-    const uint32_t en = ent[e];
-    unsigned c = (unsigned)r + (en & 0xffffu);
-    unsigned cm = c - (unsigned)z;
-    off[e] = (int)(en >> 16) * z + (int)min(c, cm);
-    float mag = (e == old_i1) ? a2 : a1;
-    uint32_t ob = __float_as_uint(mag) | ((t0 << e) & 0x80000000u);
-    x[e] = __fsub_rn(post[off[e]], __uint_as_float(ob));
+    off[e] = addr(e);
+    const float mag = (e == old_i1) ? a2 : a1;
+    const float p = ld_post(post, off[e]);
+    // p - (-mag) is p + mag, bit for bit
+    x[e] = ((t0 << e) & 0x80000000u) ? __fadd_rn(p, mag) : __fsub_rn(p, mag);
   }
-  uint32_t par = 0;
+  // m1 carries the sign product (xor of the signs of all x) in its sign bit
   float m1 = infinity<float>(), m2 = infinity<float>();
 #pragma unroll
-  for (int e = 0; e < D; e++) {
-    par ^= __float_as_uint(x[e]);
-    float av = fabsf(x[e]);
-    m2 = fminf(m2, fmaxf(m1, av));
-    m1 = fminf(m1, av);
+  for (int e = 0; e + 1 < D; e += 2) {
+    const float s = min_xorsign_abs(x[e], x[e + 1]);
+    const float l = fmaxf(fabsf(x[e]), fabsf(x[e + 1]));
+    m2 = min3f(m2, fmaxf(fabsf(m1), fabsf(s)), l);
+    m1 = min_xorsign_abs(m1, s);
   }
+  if (D & 1) {
+    m2 = fminf(m2, fmaxf(fabsf(m1), fabsf(x[D - 1])));
+    m1 = min_xorsign_abs(m1, x[D - 1]);
+  }
+  const uint32_t ps = __float_as_uint(m1) & 0x80000000u;
+  m1 = fabsf(m1);
   if (rule == cbd::RULE_NMS) {
     n1 = __fmul_rn(alpha, m1);
     n2 = __fmul_rn(alpha, m2);
@@ -211,20 +260,36 @@ __device__ __forceinline__ void row_update_lean(float* __restrict__ post, const 
     n1 = fmaxf(__fsub_rn(m1, alpha), 0.0f);
     n2 = fmaxf(__fsub_rn(m2, alpha), 0.0f);
   }
-  const uint32_t ps = par & 0x80000000u;
   const uint32_t n1p = __float_as_uint(n1) | ps, n2p = __float_as_uint(n2) | ps;
   uint32_t sm = 0;
   int i1 = 0;
 #pragma unroll
   for (int e = 0; e < D; e++) {
-    bool eq = fabsf(x[e]) == m1;
-    uint32_t magp = eq ? n2p : n1p;
+    const bool eq = fabsf(x[e]) == m1;
+    const uint32_t magp = eq ? n2p : n1p;
     i1 = eq ? e : i1;
-    uint32_t ob = magp ^ (__float_as_uint(x[e]) & 0x80000000u);
-    post[off[e]] = __fadd_rn(x[e], __uint_as_float(ob));
+    const uint32_t ob = magp ^ (__float_as_uint(x[e]) & 0x80000000u);
+    st_post(post, off[e], __fadd_rn(x[e], __uint_as_float(ob)));
     sm = (sm << 1) | (ob >> 31);
   }
   nm = (sm << 8) | (uint32_t)i1;
+}
+
+template <typename Addr>
+__device__ __forceinline__ void row_dispatch_lean(int d, float* post, const Addr& addr, float a1, float a2,
+                                                  uint32_t mt, int rule, float alpha, float& n1, float& n2,
+                                                  uint32_t& nm) {
+  switch (d) {
+    case 3: row_update_lean<3>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 4: row_update_lean<4>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 5: row_update_lean<5>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 6: row_update_lean<6>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 7: row_update_lean<7>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 8: row_update_lean<8>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 9: row_update_lean<9>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 10: row_update_lean<10>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    default: row_update_lean<19>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+  }
 }
 
 template <typename T>
@@ -232,17 +297,7 @@ __device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent
                                              uint32_t mt, int rule, T alpha, T& n1, T& n2, uint32_t& nm) {
 #ifndef CB_F32_CLASSIC_ROWS
   if constexpr (sizeof(T) == 4) {
-    switch (d) {
-      case 3: row_update_lean<3>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-      case 4: row_update_lean<4>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-      case 5: row_update_lean<5>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-      case 6: row_update_lean<6>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-      case 7: row_update_lean<7>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-      case 8: row_update_lean<8>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-      case 9: row_update_lean<9>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-      case 10: row_update_lean<10>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-      default: row_update_lean<19>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    }
+    row_dispatch_lean(d, post, EdgeAddrPacked{ent, r, z}, a1, a2, mt, rule, alpha, n1, n2, nm);
     return;
   }
 #endif

@@ -25,7 +25,11 @@ inline void fill_dev_code(const cbh::NrCode& h, cbd::DevCode& v) {
   v.map_is_offset = h.map_is_offset;
   v.has_repeats = h.has_repeats;
   for (int i = 0; i <= h.rows_n; i++) v.layer_start[i] = (uint16_t)h.layer_start[i];
-  for (int t = 0; t < v.n_entries; t++) v.entry[t] = ((uint32_t)h.entry_col[t] << 16) | h.entry_shift[t];
+  for (int t = 0; t < v.n_entries; t++) {
+    v.entry[t] = ((uint32_t)h.entry_col[t] << 16) | h.entry_shift[t];
+    v.eaddr[t].x = 4u * ((uint32_t)h.entry_col[t] * (uint32_t)h.z + h.entry_shift[t]);
+    v.eaddr[t].y = (uint32_t)h.z - h.entry_shift[t];
+  }
   for (int t = 0; t < v.n_core_terms; t++)
     v.core_term[t] = ((uint32_t)h.core_terms[t].block << 20) | ((uint32_t)h.core_terms[t].src << 16) |
                      h.core_terms[t].shift;

@@ -1,6 +1,8 @@
 // Shared device-side pieces: the per-frame xoshiro256** streams, the code descriptor
 // handed to every kernel, and the per-frame result record.
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 #include "code_host.h"
@@ -93,6 +95,7 @@ struct DevCode {
   uint16_t layer_start[cbh::kMaxLayers + 1];
   uint32_t entry[cbh::kMaxEntries];      // (base column << 16) | shift
   uint32_t core_term[cbh::kMaxCoreTerms];  // (block << 20) | (src << 16) | shift
+  uint2 eaddr[cbh::kMaxEntries];           // {4 (column Z + shift), Z - shift}
 };
 
 // decoder settings (crates/com-fec/src/ldpc.rs:165-172)
