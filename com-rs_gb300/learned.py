@@ -83,7 +83,7 @@ PROTOCOLS = {
     # the configured grid 2:0.1:4 dB lies below this code's waterfall (about 6.3 dB at 20
     # iterations, 7 dB at 8: 64-QAM at rate 1/2 without a bit interleaver, max-log LLRs), so
     # FER = 1 there for every decoder; the network is trained and compared on the waterfall
-    "c5": dict(k=8448, e=16896, bg=1, z=384, m=64, T=8, shared=True, lo=6.0, hi=7.5, steps=800, batch=256,
+    "c5": dict(k=8448, e=16896, bg=1, z=384, m=64, T=8, shared=True, lo=6.0, hi=7.5, steps=3200, batch=1024,
                grid=[6.0 + 0.1 * i for i in range(16)], plain=(8, 20), min_errors=100, max_frames=1_000_000,
                configured_grid=[2.0 + 0.1 * i for i in range(21)]),
 }
