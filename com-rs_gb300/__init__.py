@@ -8,6 +8,8 @@ the reference's Python surface for this path:
   ``decode`` / ``app``, plus the explicit ``lifting_size`` and the GPU ``precision``;
 * :meth:`NrLdpc.run_frames` -- the Monte Carlo frames of one condition, frame f drawn
   from ``stream(seed, name, condition, f)`` (crates/com-sim/src/runner.rs:435-447);
+* :class:`Ldpc` -- the reference's generic ``LdpcCode`` decoder (any parity-check matrix,
+  alist files, sum-product or min-sum, layered or flooding; crates/com-fec/src/ldpc.rs);
 * :func:`run` -- a campaign over an Eb/N0 grid with the ``min_errors(...).or(max_trials)``
   stopping rule of com-sim (crates/com-sim/src/stopping.rs:64-265).
 
@@ -21,6 +23,7 @@ import os
 import numpy as np
 
 from .campaign import Grid, Stop, run  # noqa: F401
+from .ldpc import Ldpc, parse_alist  # noqa: F401
 from .mix import MIX_ITEM_DTYPE, MixBatch, autotune, draw_mixed_batch  # noqa: F401
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -83,6 +86,13 @@ SYMBOLS = [
     ("cb_mix_time_decode", _i32, [_vp, _i32, _i32, C.POINTER(_dbl)]),
     ("cb_decode_device_noalloc", _i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
     ("cb_xoshiro_jump", _i32, [_vp, _u64, _vp]),
+    ("cb_ldpc_create", _i32, [_i32, _i32, _vp, _vp, _i32, _dbl, _i32, _i32, _i32, _i32, C.POINTER(_vp)]),
+    ("cb_ldpc_destroy", None, [_vp]),
+    ("cb_ldpc_last_error", C.c_char_p, [_vp]),
+    ("cb_ldpc_info", _i32, [_vp, _vp]),
+    ("cb_ldpc_levels", _i32, [_vp, _vp, _vp]),
+    ("cb_ldpc_decode", _i32, [_vp, _vp, _i64, _vp, _vp]),
+    ("cb_ldpc_decode_device", _i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
 ]
 
 _lib = None

@@ -88,10 +88,10 @@ cb_status cuda_fail(cb_code* c, cudaError_t e, const char* what) {
 template <typename P>
 cudaError_t grow(P*& ptr, size_t& cap, size_t bytes) {
   if (bytes <= cap) return cudaSuccess;
+  const size_t want = std::max(bytes, cap * 3 / 2);
   if (ptr) cudaFree((void*)ptr);
   ptr = nullptr;
   cap = 0;
-  size_t want = std::max(bytes, cap * 3 / 2);
   cudaError_t e = cudaMalloc((void**)&ptr, want);
   if (e == cudaSuccess) cap = want;
   return e;

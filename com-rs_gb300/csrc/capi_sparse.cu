@@ -1,0 +1,251 @@
+// The C ABI of generic sparse LDPC codes (cb_ldpc_* of include/comrs_gb300.h):
+// LdpcCode::decode_llr (crates/com-fec/src/ldpc.rs:497-505) on the GPU for any
+// parity-check matrix, with the decoder settings of LdpcDecoder (ldpc.rs:165-172).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <string>
+
+#include "../../include/comrs_gb300.h"
+#include "kernels.h"
+#include "sparse_host.h"
+
+namespace {
+
+thread_local std::string g_ldpc_thread_error;
+
+// shared memory the edge messages may take before they move to global slots: keeps
+// two CTAs resident per SM
+constexpr size_t kSmemMsgBudget = 100 * 1024;
+
+}  // namespace
+
+struct cb_ldpc {
+  std::mutex mu;
+  int device = 0, precision = 0, rule = 0, layered = 1, max_iterations = 0;
+  double alpha = 0;
+  cbh::SparseCode host;
+  bool dev_ready = false;
+  cbk::SparseDev dev{};
+  int32_t* d_tables = nullptr;
+  unsigned long long* d_counter = nullptr;
+  void* d_slots = nullptr;
+  int grid = 0, threads = 0;
+  size_t smem = 0;
+  bool msgs_in_smem = false;
+  void* kernel = nullptr;
+  cudaStream_t stream = nullptr;
+  void* d_llr = nullptr;
+  size_t llr_cap = 0;
+  void* d_post = nullptr;
+  size_t post_cap = 0;
+  int32_t* d_iters = nullptr;
+  size_t iters_cap = 0;
+  std::string err;
+};
+
+namespace {
+
+cb_status lfail(cb_ldpc* c, cb_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  g_ldpc_thread_error = msg;
+  return s;
+}
+
+#define LDPC_CUDA(c, call)                                                                      \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) return lfail((c), CB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+cudaError_t grow_buf(void** ptr, size_t& cap, size_t bytes) {
+  if (bytes <= cap) return cudaSuccess;
+  const size_t want = std::max(bytes, cap * 3 / 2);
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc(ptr, want);
+  if (e == cudaSuccess) cap = want;
+  return e;
+}
+
+size_t elem(const cb_ldpc* c) { return c->precision == CB_F64 ? 8 : 4; }
+
+// device tables, launch shape and message storage, on first use
+cb_status ensure_device(cb_ldpc* c) {
+  if (c->dev_ready) return CB_OK;
+  const cbh::SparseCode& h = c->host;
+  LDPC_CUDA(c, cudaSetDevice(c->device));
+  if (!c->stream) LDPC_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  const size_t words = h.row_start.size() + h.vars.size() + h.col_start.size() + h.col_edges.size() +
+                       h.level_start.size() + h.level_rows.size();
+  LDPC_CUDA(c, cudaMalloc(&c->d_tables, words * 4));
+  int32_t* p = c->d_tables;
+  auto put = [&](const std::vector<int32_t>& v, const int32_t*& dst) -> cudaError_t {
+    dst = p;
+    cudaError_t e = cudaMemcpy(p, v.data(), v.size() * 4, cudaMemcpyHostToDevice);
+    p += v.size();
+    return e;
+  };
+  cbk::SparseDev& d = c->dev;
+  d.n = h.n;
+  d.m = h.m;
+  d.edges = h.edges;
+  d.levels = h.levels;
+  LDPC_CUDA(c, put(h.row_start, d.row_start));
+  LDPC_CUDA(c, put(h.vars, d.vars));
+  LDPC_CUDA(c, put(h.col_start, d.col_start));
+  LDPC_CUDA(c, put(h.col_edges, d.col_edges));
+  LDPC_CUDA(c, put(h.level_start, d.level_start));
+  LDPC_CUDA(c, put(h.level_rows, d.level_rows));
+  LDPC_CUDA(c, cudaMalloc(&c->d_counter, sizeof(unsigned long long)));
+  // threads: a level's rows (layered) or a share of the rows and variables (flooding)
+  const int want = c->layered ? h.max_level_rows : std::max(h.m, h.n) / 4;
+  c->threads = std::min(512, std::max(64, (want + 31) / 32 * 32));
+  const size_t post_bytes = (size_t)h.n * elem(c);
+  const size_t msg_bytes = (size_t)2 * h.edges * elem(c);
+  c->msgs_in_smem = post_bytes + msg_bytes <= kSmemMsgBudget;
+  c->smem = (post_bytes + (c->msgs_in_smem ? msg_bytes : 0) + 15) & ~(size_t)15;
+  if (c->smem > 227 * 1024) return lfail(c, CB_ERR_CONFIG, "the posteriors of this code do not fit in shared memory");
+  c->kernel = cbk::sparse_kernel_ptr(c->precision == CB_F64 ? 0 : 1, c->rule, c->layered != 0);
+  LDPC_CUDA(c, cudaFuncSetAttribute(c->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+  int per_sm = 0, sms = 0;
+  LDPC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c->kernel, c->threads, c->smem));
+  LDPC_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  c->grid = std::max(1, per_sm * sms);
+  if (!c->msgs_in_smem) LDPC_CUDA(c, cudaMalloc(&c->d_slots, (size_t)c->grid * msg_bytes));
+  c->dev_ready = true;
+  return CB_OK;
+}
+
+template <typename T>
+cb_status decode_impl(cb_ldpc* c, const T* llr, int64_t n, T* post, int32_t* iters, cudaStream_t s) {
+  if (n == 0) return CB_OK;
+  cbk::SparseArgs<T> a;
+  a.code = c->dev;
+  a.alpha = c->alpha;
+  a.max_iterations = c->max_iterations;
+  a.msgs_in_smem = c->msgs_in_smem ? 1 : 0;
+  a.llr = llr;
+  a.n_frames = n;
+  a.post_out = post;
+  a.iters_out = iters;
+  a.slots = reinterpret_cast<T*>(c->d_slots);
+  a.work_counter = c->d_counter;
+  LDPC_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), s));
+  const int grid = (int)std::min<int64_t>(c->grid, n);
+  LDPC_CUDA(c, cbk::launch_sparse(c->kernel, &a, grid, c->threads, c->smem, s));
+  return CB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cb_status cb_ldpc_create(int32_t n, int32_t m, const int32_t* row_start, const int32_t* vars, int32_t rule,
+                         double alpha, int32_t layered, int32_t max_iterations, int32_t precision, int32_t device,
+                         cb_ldpc** out) {
+  if (!out) return lfail(nullptr, CB_ERR_CONFIG, "null output pointer");
+  *out = nullptr;
+  if (rule != CB_RULE_SUM_PRODUCT && rule != CB_RULE_NMS && rule != CB_RULE_OMS)
+    return lfail(nullptr, CB_ERR_CONFIG, "rule must be sum-product, normalised or offset min-sum");
+  if (max_iterations < 0) return lfail(nullptr, CB_ERR_CONFIG, "max_iterations must be >= 0");
+  if (precision != CB_F64 && precision != CB_F32) return lfail(nullptr, CB_ERR_CONFIG, "precision must be f64 or f32");
+  if (!std::isfinite(alpha)) return lfail(nullptr, CB_ERR_CONFIG, "alpha must be finite");
+  cb_ldpc* c = new cb_ldpc;
+  std::string err;
+  if (!cbh::build_sparse_code(n, m, row_start, vars, c->host, err)) {
+    delete c;
+    return lfail(nullptr, CB_ERR_CONFIG, err);
+  }
+  c->device = device;
+  c->precision = precision;
+  c->rule = rule;
+  c->alpha = alpha;
+  c->layered = layered ? 1 : 0;
+  c->max_iterations = max_iterations;
+  *out = c;
+  return CB_OK;
+}
+
+void cb_ldpc_destroy(cb_ldpc* c) {
+  if (!c) return;
+  if (c->dev_ready || c->stream) {
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_tables);
+    cudaFree(c->d_counter);
+    cudaFree(c->d_slots);
+    cudaFree(c->d_llr);
+    cudaFree(c->d_post);
+    cudaFree(c->d_iters);
+    if (c->stream) cudaStreamDestroy(c->stream);
+  }
+  delete c;
+}
+
+const char* cb_ldpc_last_error(const cb_ldpc* c) { return c ? c->err.c_str() : g_ldpc_thread_error.c_str(); }
+
+cb_status cb_ldpc_info(const cb_ldpc* c, int64_t* info) {
+  if (!c || !info) return lfail(nullptr, CB_ERR_CONFIG, "null argument");
+  const cbh::SparseCode& h = c->host;
+  const int64_t v[8] = {h.n, h.m, h.edges, h.max_row_degree, h.max_col_degree, h.levels, h.max_level_rows,
+                        c->layered};
+  std::copy(v, v + 8, info);
+  return CB_OK;
+}
+
+cb_status cb_ldpc_levels(const cb_ldpc* c, int32_t* level_start, int32_t* level_rows) {
+  if (!c) return lfail(nullptr, CB_ERR_CONFIG, "null argument");
+  if (level_start) std::copy(c->host.level_start.begin(), c->host.level_start.end(), level_start);
+  if (level_rows) std::copy(c->host.level_rows.begin(), c->host.level_rows.end(), level_rows);
+  return CB_OK;
+}
+
+cb_status cb_ldpc_decode_device(cb_ldpc* c, const void* llr, int64_t n_frames, void* post, int32_t* iterations,
+                                void* stream) {
+  if (!c) return lfail(nullptr, CB_ERR_CONFIG, "null code");
+  if (n_frames < 0) return lfail(c, CB_ERR_SHAPE, "n_frames must be >= 0");
+  if (n_frames > 0 && !llr) return lfail(c, CB_ERR_SHAPE, "null LLRs");
+  std::lock_guard<std::mutex> lock(c->mu);
+  if (cb_status st = ensure_device(c)) return st;
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  if (c->precision == CB_F64)
+    return decode_impl<double>(c, (const double*)llr, n_frames, (double*)post, iterations, s);
+  return decode_impl<float>(c, (const float*)llr, n_frames, (float*)post, iterations, s);
+}
+
+cb_status cb_ldpc_decode(cb_ldpc* c, const void* llr, int64_t n_frames, void* post, int32_t* iterations) {
+  if (!c) return lfail(nullptr, CB_ERR_CONFIG, "null code");
+  if (n_frames < 0) return lfail(c, CB_ERR_SHAPE, "n_frames must be >= 0");
+  if (n_frames == 0) return CB_OK;
+  if (!llr) return lfail(c, CB_ERR_SHAPE, "null LLRs");
+  std::lock_guard<std::mutex> lock(c->mu);
+  if (cb_status st = ensure_device(c)) return st;
+  const size_t per = (size_t)c->host.n * elem(c);
+  // chunks of at most 1 GB of LLRs
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n_frames, (int64_t)(((size_t)1 << 30) / per)));
+  LDPC_CUDA(c, grow_buf(&c->d_llr, c->llr_cap, chunk * per));
+  if (post) LDPC_CUDA(c, grow_buf(&c->d_post, c->post_cap, chunk * per));
+  if (iterations) LDPC_CUDA(c, grow_buf((void**)&c->d_iters, c->iters_cap, chunk * 4));
+  for (int64_t f0 = 0; f0 < n_frames; f0 += chunk) {
+    const int64_t k = std::min(chunk, n_frames - f0);
+    LDPC_CUDA(c, cudaMemcpyAsync(c->d_llr, (const char*)llr + f0 * per, k * per, cudaMemcpyHostToDevice, c->stream));
+    cb_status st = c->precision == CB_F64
+                       ? decode_impl<double>(c, (const double*)c->d_llr, k, post ? (double*)c->d_post : nullptr,
+                                             iterations ? c->d_iters : nullptr, c->stream)
+                       : decode_impl<float>(c, (const float*)c->d_llr, k, post ? (float*)c->d_post : nullptr,
+                                            iterations ? c->d_iters : nullptr, c->stream);
+    if (st) return st;
+    if (post)
+      LDPC_CUDA(c, cudaMemcpyAsync((char*)post + f0 * per, c->d_post, k * per, cudaMemcpyDeviceToHost, c->stream));
+    if (iterations)
+      LDPC_CUDA(c, cudaMemcpyAsync(iterations + f0, c->d_iters, k * 4, cudaMemcpyDeviceToHost, c->stream));
+    LDPC_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return CB_OK;
+}
+
+}  // extern "C"

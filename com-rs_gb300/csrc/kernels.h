@@ -154,4 +154,31 @@ cudaError_t launch_adam(float* w, const float* g, float* m, float* v, int64_t n,
 template <typename T>
 cudaError_t launch_gen(const GenArgs<T>& a, cudaStream_t stream);
 
+// ---- generic sparse codes (sparse.cu)
+struct SparseDev {
+  int32_t n, m, edges, levels;
+  const int32_t* row_start;    // m + 1
+  const int32_t* vars;         // edges
+  const int32_t* col_start;    // n + 1
+  const int32_t* col_edges;    // edges, per variable in row order
+  const int32_t* level_start;  // levels + 1
+  const int32_t* level_rows;   // m
+};
+template <typename T>
+struct SparseArgs {
+  SparseDev code;
+  double alpha;  // NMS scale or OMS offset
+  int32_t max_iterations;
+  int32_t msgs_in_smem;  // 1: the edge messages live in shared memory, else in `slots`
+  const T* llr;          // [n_frames][n]
+  int64_t n_frames;
+  T* post_out;           // [n_frames][n] (nullable)
+  int32_t* iters_out;    // [n_frames] (nullable)
+  T* slots;              // [grid][2][edges] when !msgs_in_smem
+  unsigned long long* work_counter;
+};
+// the kernel of a precision (0: f64, 1: f32), rule and schedule
+void* sparse_kernel_ptr(int precision, int rule, bool layered);
+cudaError_t launch_sparse(void* kernel, const void* args, int grid, int threads, size_t smem, cudaStream_t stream);
+
 }  // namespace cbk

@@ -1,0 +1,219 @@
+// Belief propagation on a generic sparse LDPC code: the propagate loop of LdpcCode
+// (crates/com-fec/src/ldpc.rs:509-557) with the three check rules of check_message
+// (:449-493) and both schedules, for any parity-check matrix (PEG, alist, IRA, DVB-S2,
+// or the lifted rows of a 5G NR code).
+//
+// One CTA decodes one codeword at a time (a persistent grid with an atomic work
+// counter).  The posteriors sit in shared memory; the check-to-variable messages, one
+// per edge as in the reference, sit in shared memory when they fit and otherwise in the
+// CTA's slot of a global buffer.
+//
+//   * Layered: the rows run level by level (the level schedule of sparse_host.h), one
+//     thread per row of the level, a barrier between levels.  This is the reference's
+//     sequential row order exactly.
+//   * Flooding: every row computes its new messages from the previous posteriors; then
+//     every variable sums the channel LLR and its new messages in increasing row order,
+//     as the reference's loop over the rows does.
+//
+// Every step is an explicitly rounded IEEE operation in the reference's order.  The
+// min-sum rules are therefore bit-exact in f64 (and equal to the same algorithm in f32).
+// The sum-product rule calls CUDA's tanh and atanh where the reference calls the
+// platform libm: results agree to rounding, not bit for bit.
+#include <cuda_runtime.h>
+
+#include "decode_common.cuh"
+#include "kernels.h"
+
+namespace cbk {
+namespace {
+
+// TANH_BOUND of ldpc.rs:37; it rounds to 1 in f32, where the bound is the largest
+// float below 1 (1 - 2^-24)
+template <typename T>
+__device__ __forceinline__ T tanh_bound();
+template <>
+__device__ __forceinline__ double tanh_bound<double>() { return 0.999999999999; }
+template <>
+__device__ __forceinline__ float tanh_bound<float>() { return __uint_as_float(0x3f7fffffu); }
+
+__device__ __forceinline__ double tanh_t(double x) { return tanh(x); }
+__device__ __forceinline__ float tanh_t(float x) { return tanhf(x); }
+__device__ __forceinline__ double atanh_t(double x) { return atanh(x); }
+__device__ __forceinline__ float atanh_t(float x) { return atanhf(x); }
+
+// f64::clamp(lo, hi)
+template <typename T>
+__device__ __forceinline__ T clamp_t(T x, T lo, T hi) {
+  return x < lo ? lo : (x > hi ? hi : x);
+}
+
+// One check node.  in(i): the incoming message of edge i (post - c2v, recomputed on
+// each pass, always to the same value).  Layered: the outputs go to msg (replacing the
+// old messages after they are read) and to post; flooding: to out only.  aux holds the
+// prefix products of the sum-product rule.
+template <typename T, int RULE, bool LAYERED>
+__device__ __forceinline__ void check_row(const SparseDev& c, int row, T* post, T* msg, T* out, T* aux, T alpha) {
+  const int e0 = c.row_start[row], e1 = c.row_start[row + 1];
+  if (RULE == cbd::RULE_SUM_PRODUCT) {
+    // the product of the other tanh(L/2) by prefix and suffix products
+    T prefix = (T)1;
+    for (int e = e0; e < e1; e++) {
+      const T l = sub_rn(post[c.vars[e]], msg[e]);
+      const T t = tanh_t(mul_rn(l, (T)0.5));
+      aux[e] = prefix;
+      prefix = mul_rn(prefix, t);
+    }
+    T suffix = (T)1;
+    for (int e = e1 - 1; e >= e0; e--) {
+      const int v = c.vars[e];
+      const T l = sub_rn(post[v], msg[e]);
+      const T t = tanh_t(mul_rn(l, (T)0.5));
+      const T p = mul_rn(aux[e], suffix);
+      suffix = mul_rn(suffix, t);
+      const T o = mul_rn((T)2, atanh_t(clamp_t(p, -tanh_bound<T>(), tanh_bound<T>())));
+      if (LAYERED) {
+        msg[e] = o;
+        post[v] = add_rn(l, o);
+      } else {
+        out[e] = o;
+      }
+    }
+  } else {
+    int neg = 0, i1 = 0;
+    T m1 = infinity<T>(), m2 = infinity<T>();
+    for (int e = e0, i = 0; e < e1; e++, i++) {
+      const T l = sub_rn(post[c.vars[e]], msg[e]);
+      neg ^= (int)(l < (T)0);
+      const T a = fabs(l);
+      if (a < m1) {
+        m2 = m1;
+        m1 = a;
+        i1 = i;
+      } else if (a < m2) {
+        m2 = a;
+      }
+    }
+    const T sign = neg ? (T)-1 : (T)1;
+    for (int e = e0, i = 0; e < e1; e++, i++) {
+      const int v = c.vars[e];
+      const T l = sub_rn(post[v], msg[e]);
+      const T s = mul_rn(sign, l < (T)0 ? (T)-1 : (T)1);
+      T mag = i == i1 ? m2 : m1;
+      mag = RULE == cbd::RULE_NMS ? mul_rn(alpha, mag) : fmax(sub_rn(mag, alpha), (T)0);
+      const T o = mul_rn(s, mag);
+      if (LAYERED) {
+        msg[e] = o;
+        post[v] = add_rn(l, o);
+      } else {
+        out[e] = o;
+      }
+    }
+  }
+}
+
+// hard_decisions_are_a_codeword (ldpc.rs:555-557), CTA-wide
+template <typename T>
+__device__ __forceinline__ bool some_row_fails(const SparseDev& c, const T* post) {
+  int bad = 0;
+  for (int r = threadIdx.x; r < c.m && !bad; r += blockDim.x) {
+    int par = 0;
+    for (int e = c.row_start[r]; e < c.row_start[r + 1]; e++) par ^= (int)(post[c.vars[e]] < (T)0);
+    bad = par;
+  }
+  return __syncthreads_or(bad) != 0;
+}
+
+template <typename T, int RULE, bool LAYERED>
+__global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ SparseArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SparseDev& c = a.code;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  T* post = reinterpret_cast<T*>(smem);
+  T* msg;
+  T* aux;
+  if (a.msgs_in_smem) {
+    msg = post + c.n;
+    aux = msg + c.edges;
+  } else {
+    msg = a.slots + (size_t)blockIdx.x * 2 * c.edges;
+    aux = msg + c.edges;
+  }
+  const T alpha = (T)a.alpha;
+  __shared__ long long s_cw;
+  for (;;) {
+    if (tid == 0) s_cw = (long long)atomicAdd(a.work_counter, 1ull);
+    __syncthreads();
+    const long long cw = s_cw;
+    if (cw >= a.n_frames) break;
+    const T* llr = a.llr + (size_t)cw * c.n;
+    for (int v = tid; v < c.n; v += nt) post[v] = llr[v];
+    for (int e = tid; e < c.edges; e += nt) {
+      msg[e] = (T)0;
+      aux[e] = (T)0;
+    }
+    __syncthreads();
+    int it = 0;
+    if (some_row_fails(c, post)) {
+      it = a.max_iterations;
+      T* cur = msg;   // flooding: the messages of the previous iteration
+      T* next = aux;  // flooding: the new ones
+      for (int iter = 1; iter <= a.max_iterations; iter++) {
+        if (LAYERED) {
+          for (int L = 0; L < c.levels; L++) {
+            const int r0 = c.level_start[L], r1 = c.level_start[L + 1];
+            for (int i = r0 + tid; i < r1; i += nt) check_row<T, RULE, true>(c, c.level_rows[i], post, msg, nullptr, aux, alpha);
+            __syncthreads();
+          }
+        } else {
+          // the sum-product rule keeps its prefix products in `next`, where its outputs go
+          for (int r = tid; r < c.m; r += nt) check_row<T, RULE, false>(c, r, post, cur, next, next, alpha);
+          __syncthreads();
+          for (int v = tid; v < c.n; v += nt) {
+            T s = llr[v];
+            for (int k = c.col_start[v]; k < c.col_start[v + 1]; k++) s = add_rn(s, next[c.col_edges[k]]);
+            post[v] = s;
+          }
+          T* t = cur;
+          cur = next;
+          next = t;
+          __syncthreads();
+        }
+        if (!some_row_fails(c, post)) {
+          it = iter;
+          break;
+        }
+      }
+    }
+    if (a.post_out)
+      for (int v = tid; v < c.n; v += nt) a.post_out[(size_t)cw * c.n + v] = post[v];
+    if (tid == 0 && a.iters_out) a.iters_out[cw] = it;
+    __syncthreads();
+  }
+}
+
+template <typename T>
+void* sparse_kernel_for(int rule, bool layered) {
+  if (layered) {
+    if (rule == cbd::RULE_SUM_PRODUCT) return (void*)sparse_kernel<T, cbd::RULE_SUM_PRODUCT, true>;
+    if (rule == cbd::RULE_NMS) return (void*)sparse_kernel<T, cbd::RULE_NMS, true>;
+    return (void*)sparse_kernel<T, cbd::RULE_OMS, true>;
+  }
+  if (rule == cbd::RULE_SUM_PRODUCT) return (void*)sparse_kernel<T, cbd::RULE_SUM_PRODUCT, false>;
+  if (rule == cbd::RULE_NMS) return (void*)sparse_kernel<T, cbd::RULE_NMS, false>;
+  return (void*)sparse_kernel<T, cbd::RULE_OMS, false>;
+}
+
+}  // namespace
+
+void* sparse_kernel_ptr(int precision, int rule, bool layered) {
+  return precision == 0 ? sparse_kernel_for<double>(rule, layered) : sparse_kernel_for<float>(rule, layered);
+}
+
+cudaError_t launch_sparse(void* kernel, const void* args, int grid, int threads, size_t smem, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* argv[] = {const_cast<void*>(args)};
+  return cudaLaunchKernel(kernel, dim3(grid), dim3(threads), argv, smem, s);
+}
+
+}  // namespace cbk

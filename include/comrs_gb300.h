@@ -198,6 +198,36 @@ cb_status cb_mix_run(cb_mix* mix, uint64_t epoch, cb_frame_result* out);
 /* the best of `reps` event-timed decode phases of one class (-1: all classes) */
 cb_status cb_mix_time_decode(cb_mix* mix, int32_t class_index, int32_t reps, double* ms);
 
+/* ---- Generic sparse LDPC codes: LdpcCode::decode_llr (crates/com-fec/src/ldpc.rs:497-505)
+ * for any parity-check matrix given by its rows (LdpcCode::from_rows / from_alist,
+ * ldpc.rs:222-239, :350-370; PEG, IRA and DVB-S2 codes, or the lifted rows of an NR
+ * code), with the decoder settings of LdpcDecoder (ldpc.rs:165-172): the sum-product,
+ * normalised or offset min-sum rule (check_message, ldpc.rs:449-493), the layered or
+ * flooding schedule (propagate, ldpc.rs:509-553).  Row r lists its variables at
+ * vars[row_start[r] .. row_start[r + 1]) (0-based; each at most once per row); its
+ * messages follow that order, as the reference's edges do.  The min-sum rules are
+ * bit-exact in f64; the sum-product rule calls CUDA's tanh/atanh where the reference
+ * calls the platform libm.  Device resources are made on the first decode. */
+typedef struct cb_ldpc cb_ldpc;
+cb_status cb_ldpc_create(int32_t n, int32_t m, const int32_t* row_start, const int32_t* vars, int32_t rule,
+                         double alpha, int32_t layered, int32_t max_iterations, int32_t precision, int32_t device,
+                         cb_ldpc** out);
+void cb_ldpc_destroy(cb_ldpc* code);
+/* the last error of `code` (or of the calling thread's last cb_ldpc call when NULL) */
+const char* cb_ldpc_last_error(const cb_ldpc* code);
+/* info[0..8): n, m, edges, largest row degree, largest column degree, levels of the
+ * layered schedule, rows of its largest level, 1 if layered */
+cb_status cb_ldpc_info(const cb_ldpc* code, int64_t info[8]);
+/* the layered schedule: level_start[levels + 1] and level_rows[m] (nullable) */
+cb_status cb_ldpc_levels(const cb_ldpc* code, int32_t* level_start, int32_t* level_rows);
+/* decode n_frames words of n channel LLRs (host, f64 or f32 as the precision): the n
+ * posteriors of every frame into `post` and the iterations used into `iterations`
+ * (both host, nullable) */
+cb_status cb_ldpc_decode(cb_ldpc* code, const void* llr, int64_t n_frames, void* post, int32_t* iterations);
+/* the same on device buffers, enqueued on `stream` (NULL: the code's own stream) */
+cb_status cb_ldpc_decode_device(cb_ldpc* code, const void* llr_dev, int64_t n_frames, void* post_dev,
+                                int32_t* iterations_dev, void* stream);
+
 /* cb_decode_device for callers that cannot allocate device memory (a host framework
  * that owns all device memory through its own pool, or a real-time loop that forbids
  * cudaMalloc after start-up).  No counterpart in the reference: it is an addition of

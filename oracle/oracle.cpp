@@ -315,7 +315,9 @@ static void check_message(const Code& c, const T* incoming, T* out, int d, std::
     for (int i = d - 1; i >= 0; i--) {
       T p = out[i] * suffix;
       suffix *= scratch[i];
-      T cl = std::min(std::max(p, (T)-TANH_BOUND), (T)TANH_BOUND);
+      // TANH_BOUND rounds to 1 in f32: there the bound is the largest float below 1
+      const T bound = sizeof(T) == 4 ? (T)std::nextafter(1.0f, 0.0f) : (T)TANH_BOUND;
+      T cl = std::min(std::max(p, -bound), bound);
       out[i] = (T)2.0 * std::atanh(cl);
     }
     return;
@@ -955,6 +957,34 @@ int or_bpsk_frame(void* h, uint64_t seed, uint64_t name_hash, uint64_t cond, uin
   result[0] = be;
   result[1] = (uint32_t)it;
   return 0;
+}
+
+// the codewords and channel LLRs of frames [first, first + n) of or_bpsk_frame's link
+// (frame f draws from stream(seed, name_hash, cond, f)), `threads` threads
+void or_bpsk_llr_batch(void* h, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first, int64_t n,
+                       double noise_var, int threads, uint8_t* cw_out, double* llr_out) {
+  const Code* c = (const Code*)h;
+  auto work = [&](int64_t f0, int64_t f1) {
+    std::vector<uint8_t> u(c->k);
+    for (int64_t f = f0; f < f1; f++) {
+      Rng rng = stream(seed, name_hash, cond, first + (uint64_t)f);
+      uint8_t* cw = cw_out + f * c->n;
+      double* llr = llr_out + f * c->n;
+      for (int i = 0; i < c->k; i++) u[i] = rng.bit();
+      if (c->core) encode_core(*c, u.data(), cw);
+      else encode_sums(*c, u.data(), cw);
+      const double s = std::sqrt(noise_var);
+      for (int v = 0; v < c->n; v++) {
+        double x = 1.0 - 2.0 * (double)cw[v];
+        double y = x + s * rng.gaussian();
+        llr[v] = 2.0 * y / noise_var;
+      }
+    }
+  };
+  threads = std::max(1, threads);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < threads; t++) pool.emplace_back(work, n * t / threads, n * (t + 1) / threads);
+  for (auto& th : pool) th.join();
 }
 
 // learned min-sum: forward (post_out n_full, optional) and gradients (ga/gb, optional,

@@ -54,6 +54,7 @@ def lib():
         L.or_encode_full.argtypes = [vp, vp, vp]
         L.or_is_codeword.restype = i32
         L.or_is_codeword.argtypes = [vp, vp]
+        L.or_bpsk_llr_batch.argtypes = [vp, u64, u64, u64, u64, i64, dbl, i32, vp, vp]
         for f in (L.or_decode_f64, L.or_decode_f32):
             f.restype = i32
             f.argtypes = [vp, vp, vp, vp, vp]
@@ -220,6 +221,25 @@ class Code:
 
     def learned_num_weights(self, T, shared):
         return int(lib().or_learned_num_weights(self.h, T, int(shared)))
+
+    def bpsk_llr(self, seed, name_hash, cond, first, n, noise_var, threads=None):
+        """(codewords [n][n_full] u8, channel LLRs [n][n_full] f64) of bpsk_frame's frames."""
+        cw = np.zeros((n, self.n_full), np.uint8)
+        llr = np.zeros((n, self.n_full), np.float64)
+        lib().or_bpsk_llr_batch(self.h, seed, name_hash, cond, first, n, noise_var, threads or os.cpu_count() or 1,
+                                _p(cw), _p(llr))
+        return cw, llr
+
+    def decode_llr_many(self, full, precision="f64"):
+        """decode_llr of every row: (posteriors, iterations)."""
+        dt = np.float64 if precision == "f64" else np.float32
+        full = np.ascontiguousarray(full, dt).reshape(-1, self.n_full)
+        post = np.zeros_like(full)
+        its = np.zeros(full.shape[0], np.int32)
+        f = lib().or_decode_llr_f64 if precision == "f64" else lib().or_decode_llr_f32
+        for i in range(full.shape[0]):
+            its[i] = f(self.h, _p(full[i]), _p(post[i]))
+        return post, its
 
     def bpsk_frame(self, seed, name_hash, cond, trial, noise_var):
         res = np.zeros(2, np.uint32)

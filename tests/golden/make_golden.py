@@ -8,9 +8,13 @@ Outputs (committed):
     fixture ``tests/oracle/sionna_vectors.npz`` (keys ``ldpc.k{K}_n{E}.{u,c}``,
     Apache-2.0, provenance in ``tests/oracle/sionna_vectors.json`` of com-rs), stored
     with np.packbits along the last axis (shape kept in ``<key>.shape``);
-  * ``aff3ct_peg_n576_k288_layered_nms075_i20.json`` -- the AFF3CT FER/BER curve of the
-    layered normalised min-sum (alpha 0.75, 20 iterations) on the PEG(576, 288) matrix
-    (``validation/aff3ct/`` of com-rs), and ``peg_n576_k288.alist``, its matrix.
+  * the AFF3CT FER/BER curves of the LDPC decoders on com-rs's PEG matrices
+    (``validation/aff3ct/`` of com-rs): ``ldpc_peg_n576_k288_layered_nms075_i20.json``
+    (layered normalised min-sum 0.75, 20 iterations), ``..._flooding_oms015_i20.json``
+    (flooding offset min-sum 0.15), ``..._flooding_spa_i50.json`` (flooding
+    sum-product, 50 iterations) and ``ldpc_peg_n648_k540_layered_spa_i20.json``
+    (layered sum-product), with their matrices ``peg_n576_k288.alist`` and
+    ``peg_n648_k540.alist``.
 """
 
 import json
@@ -37,10 +41,11 @@ def main():
     json.dump({"source": "com-rs tests/oracle/sionna_vectors.npz", "upstream_commit": prov.get("commit"),
                "keys": sorted(k for k in out if not k.endswith(".shape"))},
               open(os.path.join(here, "sionna_nr_ldpc.json"), "w"), indent=1)
-    aff = "validation/aff3ct/ldpc_peg_n576_k288_layered_nms075_i20.json"
-    shutil.copy(os.path.join(root, aff), os.path.join(here, os.path.basename(aff)))
-    shutil.copy(os.path.join(root, "validation/aff3ct/matrices/peg_n576_k288.alist"),
-                os.path.join(here, "peg_n576_k288.alist"))
+    for name in ("ldpc_peg_n576_k288_layered_nms075_i20", "ldpc_peg_n576_k288_flooding_oms015_i20",
+                 "ldpc_peg_n576_k288_flooding_spa_i50", "ldpc_peg_n648_k540_layered_spa_i20"):
+        shutil.copy(os.path.join(root, "validation/aff3ct", name + ".json"), os.path.join(here, name + ".json"))
+    for m in ("peg_n576_k288.alist", "peg_n648_k540.alist"):
+        shutil.copy(os.path.join(root, "validation/aff3ct/matrices", m), os.path.join(here, m))
 
 
 if __name__ == "__main__":

@@ -1,0 +1,163 @@
+"""Generic sparse codes on the GPU (cb_ldpc_*) against the oracle's LdpcCode and
+against AFF3CT's recorded curves.
+
+* min-sum rules (normalised, offset; layered, flooding): posteriors equal the oracle's
+  bit for bit, f64 and f32, iterations equal;
+* sum-product: the oracle calls the platform libm's tanh/atanh, the GPU CUDA's, so the
+  comparison is statistical per frame (same decoding outcome, same iterations) and by
+  tolerance on the posteriors of frames that converge early;
+* the four LDPC fixtures of validation/tests/aff3ct.rs:219-230 (PEG(576, 288) and
+  PEG(648, 540); BPSK, sigma^2 = 1 / (2 R Eb/N0)): frame error rates whose 99 % Wilson
+  intervals overlap AFF3CT's;
+* the generic decoder on the lifted rows of an NR code equals the NR decoder.
+"""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+EBN0 = {"peg_n576_k288.alist": (1.5, 2.5), "peg_n648_k540.alist": (3.5, 4.5)}
+
+
+def _codes(cb, O, matrix, rule, alpha, layered, iters, precision):
+    text = open(os.path.join(GOLDEN, matrix)).read()
+    ref = O.Code(alist=text)
+    ref.set_decoder({"sum_product": O.RULE_SUM_PRODUCT, "normalized_min_sum": O.RULE_NMS,
+                     "offset_min_sum": O.RULE_OMS}[rule], alpha, layered, iters)
+    n, rows = cb.parse_alist(text)
+    gpu = cb.Ldpc(n, rows, rule=rule, alpha=alpha, layered=layered, max_iterations=iters, precision=precision)
+    return ref, gpu
+
+
+def _frames(O, ref, ebn0, first, n, seed=5):
+    rate = ref.k / ref.n_full
+    noise_var = 1.0 / (2.0 * rate * 10 ** (ebn0 / 10))
+    return ref.bpsk_llr(seed, O.fnv1a64("sparse"), int(ebn0 * 100), first, n, noise_var)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("rule, alpha, layered", [("normalized_min_sum", 0.75, True), ("offset_min_sum", 0.15, False),
+                                                  ("normalized_min_sum", 0.8, False), ("offset_min_sum", 0.5, True)])
+@pytest.mark.parametrize("matrix", ["peg_n576_k288.alist", "peg_n648_k540.alist"])
+def test_min_sum_equals_the_oracle_bit_for_bit(cb, O, matrix, rule, alpha, layered, precision):
+    ref, gpu = _codes(cb, O, matrix, rule, alpha, layered, 20, precision)
+    dt, it_all = (np.float64, np.uint64) if precision == "f64" else (np.float32, np.uint32), []
+    for ebn0 in EBN0[matrix]:
+        _, llr = _frames(O, ref, ebn0, 0, 200)
+        post_g, it_g = gpu.decode_llr(llr)
+        post_o, it_o = ref.decode_llr_many(llr, precision)
+        assert np.array_equal(it_g, it_o), ebn0
+        assert np.array_equal(post_g.view(dt[1]), post_o.view(dt[1])), ebn0
+        it_all.append(it_g)
+    it_all = np.concatenate(it_all)
+    assert (it_all == 20).any() and (it_all < 20).any() and len(set(it_all.tolist())) > 4
+
+
+@pytest.mark.parametrize("layered, iters", [(True, 20), (False, 50)])
+def test_sum_product_agrees_with_the_oracle(cb, O, layered, iters):
+    matrix = "peg_n576_k288.alist"
+    ref, gpu = _codes(cb, O, matrix, "sum_product", 0.0, layered, iters, "f64")
+    total = same_outcome = same_it = 0
+    worst_early = 0.0
+    for ebn0 in (1.0, 1.75, 2.5):
+        cw, llr = _frames(O, ref, ebn0, 0, 300)
+        post_g, it_g = gpu.decode_llr(llr)
+        post_o, it_o = ref.decode_llr_many(llr, "f64")
+        ok_g = ((post_g < 0) == cw.astype(bool)).all(axis=1)
+        ok_o = ((post_o < 0) == cw.astype(bool)).all(axis=1)
+        total += len(cw)
+        same_outcome += int((ok_g == ok_o).sum())
+        same_it += int((it_g == it_o).sum())
+        early = (it_g == it_o) & (it_o <= 5)
+        if early.any():
+            rel = np.abs(post_g[early] - post_o[early]) / np.maximum(1.0, np.abs(post_o[early]))
+            worst_early = max(worst_early, float(rel.max()))
+    print(f"sum-product layered={layered}: {same_outcome}/{total} same outcome, {same_it}/{total} same "
+          f"iterations, worst relative posterior gap (<= 5 iterations) {worst_early:.3g}")
+    assert same_outcome >= 0.99 * total
+    assert same_it >= 0.97 * total
+    assert worst_early <= 1e-9
+
+
+def _wilson(k, n, z=2.5758293035489004):
+    p = k / n
+    d = 1 + z * z / n
+    c = (p + z * z / (2 * n)) / d
+    h = z * np.sqrt(p * (1 - p) / n + z * z / (4 * n * n)) / d
+    return c - h, c + h
+
+
+@pytest.mark.parametrize("name, matrix, rule, alpha, layered, iters", [
+    ("ldpc_peg_n576_k288_layered_nms075_i20", "peg_n576_k288.alist", "normalized_min_sum", 0.75, True, 20),
+    ("ldpc_peg_n576_k288_flooding_oms015_i20", "peg_n576_k288.alist", "offset_min_sum", 0.15, False, 20),
+    ("ldpc_peg_n576_k288_flooding_spa_i50", "peg_n576_k288.alist", "sum_product", 0.0, False, 50),
+    ("ldpc_peg_n648_k540_layered_spa_i20", "peg_n648_k540.alist", "sum_product", 0.0, True, 20),
+])
+def test_frame_error_rates_overlap_aff3ct(cb, O, name, matrix, rule, alpha, layered, iters):
+    fx = json.load(open(os.path.join(GOLDEN, name + ".json")))
+    ref, gpu = _codes(cb, O, matrix, rule, alpha, layered, iters, "f64")
+    num, den = fx["bit_rate"]
+    rate = num / den
+    checked = 0
+    for idx, p in enumerate(fx["data"]):
+        if p["fer"] < 2e-3:
+            continue
+        noise_var = 1.0 / (2.0 * rate * 10 ** (p["ebn0_db"] / 10))
+        fe = nf = 0
+        while fe < 200 and nf < 200_000:
+            cw, llr = ref.bpsk_llr(O.fnv1a64(name), O.fnv1a64(name), idx, nf, 20_000, noise_var)
+            post, _ = gpu.decode_llr(llr)
+            fe += int((((post < 0) != cw.astype(bool)).sum(axis=1) > 0).sum())
+            nf += len(cw)
+        a_lo, a_hi = _wilson(p["frame_errors"], p["frames"])
+        c_lo, c_hi = _wilson(fe, nf)
+        assert not (a_hi < c_lo or c_hi < a_lo), (p["ebn0_db"], fe / nf, p["fer"])
+        checked += 1
+    assert checked >= 4
+
+
+def test_nr_rows_through_the_generic_decoder_equal_the_nr_decoder(cb, O):
+    # C1: BG2 Z = 52, K' = 520, E = 1040; no filler bits, so the full word is 2Z zeros,
+    # the E LLRs, then zeros for the unsent parity bits
+    nr = cb.NrLdpc(520, 1040, base_graph=2, lifting_size=52, precision="f64", max_iterations=20)
+    ref = O.Code(520, 1040, 2, 52)
+    assert (ref.n_full, ref.k) == (2704, 520)
+    r, v = ref.edges_list()
+    rows = [[] for _ in range(int(r.max()) + 1)]
+    for a, b in zip(r.tolist(), v.tolist()):
+        rows[a].append(b)
+    gpu = cb.Ldpc(ref.n_full, rows, rule="normalized_min_sum", alpha=0.75, layered=True, max_iterations=20)
+    rng = np.random.default_rng(3)
+    for ebn0 in (1.0, 2.0):
+        cw = rng.integers(0, 2, (64, 520), dtype=np.uint8)
+        sent = nr.encode(cw)
+        sigma2 = 1.0 / (2 * 0.5 * 10 ** (ebn0 / 10))
+        llr = 2 * (1 - 2.0 * sent + np.sqrt(sigma2) * rng.standard_normal(sent.shape)) / sigma2
+        full = np.zeros((64, ref.n_full))
+        full[:, 104:104 + 1040] = llr
+        post, it = gpu.decode_llr(full)
+        bits, app, it_nr = nr.decode_full(llr)
+        assert np.array_equal(it, it_nr)
+        assert np.array_equal(post[:, :520].view(np.uint64), app.view(np.uint64))
+
+
+def test_edge_cases(cb):
+    from test_sparse_host import HAMMING
+
+    n, rows = cb.parse_alist(HAMMING)
+    code = cb.Ldpc(n, rows, rule="normalized_min_sum", alpha=0.75, max_iterations=0)
+    x = np.array([1.0, -2.0, 3.0, 0.5, -0.25, 4.0, 2.0])
+    post, it = code.decode_llr(x)
+    # zero iterations: the channel LLRs come back as they are
+    assert np.array_equal(post, x) and it == 0
+    code.close()
+    code = cb.Ldpc(n, rows, rule="min_sum", max_iterations=10)
+    post, it = code.decode_llr(np.full(7, 2.0))  # the all-zero word is a codeword
+    assert it == 0 and np.array_equal(post, np.full(7, 2.0))
+    post, its = code.decode_llr(np.zeros((0, 7)))
+    assert post.shape == (0, 7) and its.shape == (0,)
