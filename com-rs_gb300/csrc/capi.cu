@@ -65,6 +65,14 @@ struct cb_code {
   std::map<int, GenCache> gen;
   bool dev_ready = false;
   std::string err;
+  // the sum-product rule and the flooding schedule: the generic decoder on the lifted rows
+  cb_ldpc* generic = nullptr;
+  void* d_full = nullptr;
+  size_t full_cap = 0;
+  void* d_post = nullptr;
+  size_t post_cap = 0;
+  int32_t* d_giters = nullptr;
+  size_t giters_cap = 0;
 };
 
 namespace {
@@ -106,9 +114,36 @@ int64_t chunk_frames(const cb_code* c) {
   return std::max<int64_t>(1, std::min<int64_t>(n, 65536));
 }
 
+// the NR word through the generic decoder: full word, decode, epilogue
+template <typename T>
+cb_status generic_decode_impl(cb_code* c, const T* llr, int64_t n, uint32_t* bits, T* app, int32_t* iters,
+                              const uint32_t* ref, cbd::FrameResult* results, cudaStream_t s) {
+  const size_t full_bytes = (size_t)n * c->host.n_full * sizeof(T);
+  CB_CUDA(c, grow(c->d_full, c->full_cap, full_bytes));
+  CB_CUDA(c, grow(c->d_post, c->post_cap, full_bytes));
+  CB_CUDA(c, grow(c->d_giters, c->giters_cap, (size_t)n * 4));
+  CB_CUDA(c, cbk::launch_full_llr<T>(c->dev, llr, n, reinterpret_cast<T*>(c->d_full), s));
+  if (cb_status st = cb_ldpc_decode_device(c->generic, c->d_full, n, c->d_post, c->d_giters, s))
+    return fail(c, st, std::string("generic decoder: ") + cb_ldpc_last_error(c->generic));
+  cbk::NrEpilogueArgs<T> e;
+  e.post = reinterpret_cast<const T*>(c->d_post);
+  e.iters_in = c->d_giters;
+  e.n_frames = n;
+  e.n_full = c->host.n_full;
+  e.k_info = c->host.k_info;
+  e.bits_out = bits;
+  e.app_out = app;
+  e.iters_out = iters;
+  e.ref_bits = ref;
+  e.results = results;
+  CB_CUDA(c, cbk::launch_nr_epilogue<T>(e, s));
+  return CB_OK;
+}
+
 template <typename T>
 cb_status decode_device_impl(cb_code* c, const T* llr, int64_t n, uint32_t* bits, T* app, int32_t* iters,
                              const uint32_t* ref, cbd::FrameResult* results, cudaStream_t s) {
+  if (c->generic) return generic_decode_impl<T>(c, llr, n, bits, app, iters, ref, results, s);
   cbk::DecodeArgs<T> a;
   a.code = c->dev;
   a.cfg = c->cfg;
@@ -326,9 +361,8 @@ cb_status cb_code_create(const cb_code_desc* d, cb_code** out) {
   *out = nullptr;
   if (!d) return fail(nullptr, CB_ERR_CONFIG, "desc is NULL");
   if (d->precision != CB_F64 && d->precision != CB_F32) return fail(nullptr, CB_ERR_CONFIG, "precision is 0 or 1");
-  if (d->rule != CB_RULE_NMS && d->rule != CB_RULE_OMS)
-    return fail(nullptr, CB_ERR_CONFIG, "the GPU decoder implements normalized_min_sum and offset_min_sum");
-  if (!d->layered) return fail(nullptr, CB_ERR_CONFIG, "the GPU decoder implements the layered schedule");
+  if (d->rule != CB_RULE_SUM_PRODUCT && d->rule != CB_RULE_NMS && d->rule != CB_RULE_OMS)
+    return fail(nullptr, CB_ERR_CONFIG, "rule must be sum_product, normalized_min_sum or offset_min_sum");
   if (d->max_iterations < 0 || d->max_iterations > 255) return fail(nullptr, CB_ERR_CONFIG, "max_iterations in 0..255");
   if (!(std::isfinite(d->alpha))) return fail(nullptr, CB_ERR_CONFIG, "alpha must be finite");
   cbh::CodeSpec spec;
@@ -356,6 +390,25 @@ cb_status cb_code_create(const cb_code_desc* d, cb_code** out) {
   c->cfg.layered = d->layered;
   c->cfg.max_iterations = d->max_iterations;
   cbk::fill_dev_code(c->host, c->dev);
+  if (d->rule == CB_RULE_SUM_PRODUCT || !d->layered) {
+    // lifted row (L, r) holds, for the entries (j, s) of base row L in table order, the
+    // variable j Z + (r + s) mod Z (nr/ldpc.rs:124-134)
+    const cbh::NrCode& h = c->host;
+    std::vector<int32_t> start(1, 0), vars;
+    vars.reserve((size_t)h.edges);
+    for (int L = 0; L < h.rows_n; L++)
+      for (int r = 0; r < h.z; r++) {
+        for (int t = h.layer_start[L]; t < h.layer_start[L + 1]; t++)
+          vars.push_back(h.entry_col[t] * h.z + (r + h.entry_shift[t]) % h.z);
+        start.push_back((int32_t)vars.size());
+      }
+    if (cb_status st = cb_ldpc_create(h.n_full, h.rows_n * h.z, start.data(), vars.data(), d->rule, d->alpha,
+                                      d->layered, d->max_iterations, d->precision, d->device, &c->generic)) {
+      std::string msg = cb_ldpc_last_error(nullptr);
+      delete c;
+      return fail(nullptr, st, msg);
+    }
+  }
   *out = c;
   return CB_OK;
 }
@@ -367,8 +420,9 @@ void cb_code_destroy(cb_code* c) {
     cudaFree(kv.second.d_points);
     cudaFree(kv.second.d_jumps);
   }
+  cb_ldpc_destroy(c->generic);
   void* bufs[] = {c->d_map, c->d_inv_start, c->d_inv_t, c->d_state, c->d_counter, c->d_status, c->d_llr, c->d_bits,
-                  c->d_info, c->d_app, c->d_iters, c->d_results, c->d_u8};
+                  c->d_info, c->d_app, c->d_iters, c->d_results, c->d_u8, c->d_full, c->d_post, c->d_giters};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -865,6 +919,8 @@ extern "C" cb_status cb_decode_device_noalloc(cb_code* c, const void* llr, int64
   if (!c->host.map_is_offset)
     return fail(c, CB_ERR_CONFIG,
                 "cb_decode_device_noalloc needs the plain rate matching (rv 0, Qm 1, no filler bits sent)");
+  if (c->generic)
+    return fail(c, CB_ERR_CONFIG, "cb_decode_device_noalloc runs the layered min-sum only");
   std::lock_guard<std::mutex> lock(c->mu);
   CB_CUDA(c, cudaSetDevice(c->device));
   if (n == 0) return CB_OK;

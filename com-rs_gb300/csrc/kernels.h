@@ -181,4 +181,22 @@ struct SparseArgs {
 void* sparse_kernel_ptr(int precision, int rule, bool layered);
 cudaError_t launch_sparse(void* kernel, const void* args, int grid, int threads, size_t smem, cudaStream_t stream);
 
+// ---- the NR code through the generic decoder (nr_generic.cu)
+template <typename T>
+struct NrEpilogueArgs {
+  const T* post;          // [n_frames][n_full]
+  const int32_t* iters_in;  // [n_frames]
+  int64_t n_frames;
+  int32_t n_full, k_info;
+  uint32_t* bits_out;       // [n_frames][ceil(K'/32)] (nullable)
+  T* app_out;               // [n_frames][K'] (nullable)
+  int32_t* iters_out;       // (nullable)
+  const uint32_t* ref_bits;   // sent info bits (nullable)
+  cbd::FrameResult* results;  // (nullable)
+};
+template <typename T>
+cudaError_t launch_full_llr(const cbd::DevCode& code, const T* llr, int64_t n_frames, T* full, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_nr_epilogue(const NrEpilogueArgs<T>& a, cudaStream_t stream);
+
 }  // namespace cbk

@@ -108,8 +108,6 @@ def test_host_encoder_on_the_sionna_vectors(cb):
     (dict(k=100, e=300, lifting_size=17), "lifting size"),
     (dict(k=8448, e=25344, base_graph=1, lifting_size=352), "systematic"),
     (dict(k=100, e=300, rule="bogus"), "rule"),
-    (dict(k=100, e=300, rule="sum_product"), "normalized_min_sum"),
-    (dict(k=100, e=300, layered=False), "layered"),
     (dict(k=100, e=300, precision="f16"), "precision"),
 ])
 def test_bad_settings_are_config_errors(cb, kw, msg):
@@ -117,6 +115,18 @@ def test_bad_settings_are_config_errors(cb, kw, msg):
     with pytest.raises(cb.ComrsError) as ei:
         cb.NrLdpc(k, e, **kw)
     assert ei.value.kind == "Config" and msg in str(ei.value)
+
+
+@pytest.mark.skipif(gpu_available(), reason="checks the behaviour without a GPU")
+@pytest.mark.parametrize("kw", [dict(rule="sum_product"), dict(layered=False), dict(rule="offset_min_sum", alpha=0.5,
+                                                                                  layered=False)])
+def test_sum_product_and_flooding_codes_build_and_fail_loudly_without_a_gpu(cb, kw):
+    # these settings run on the generic sparse decoder over the lifted rows
+    code = cb.NrLdpc(520, 1040, base_graph=2, lifting_size=52, **kw)
+    assert (code.z, code.n_full) == (52, 2704)
+    with pytest.raises(cb.ComrsError) as ei:
+        code.decode(np.zeros(1040))
+    assert ei.value.kind == "Cuda"
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the behaviour without a GPU")
