@@ -59,6 +59,7 @@ SYMBOLS = [
     ("cb_code_create", _i32, [C.POINTER(_Desc), C.POINTER(_vp)]),
     ("cb_code_destroy", None, [_vp]),
     ("cb_last_error", C.c_char_p, [_vp]),
+    ("cb_code_set_demapper", _i32, [_vp, _i32]),
     ("cb_code_info", _i32, [_vp, _vp]),
     ("cb_code_tables", _i32, [_vp, _vp, _vp]),
     ("cb_encode", _i32, [_vp, _vp, _i64, _vp]),
@@ -155,7 +156,8 @@ class NrLdpc:
     """
 
     def __init__(self, k, e, base_graph=None, rv=0, qm=1, rule="normalized_min_sum", alpha=0.75,
-                 max_iterations=20, layered=True, lifting_size=None, precision="f64", device=0):
+                 max_iterations=20, layered=True, lifting_size=None, precision="f64", device=0,
+                 demapper="max_log"):
         rule_l = rule.lower()
         if rule_l not in RULES:
             raise ComrsError(-1, f"rule must be one of {sorted(RULES)}, got {rule!r}")
@@ -172,6 +174,10 @@ class NrLdpc:
         (self.bg, self.z, self.k_info, self.e, self.k_sys, self.n_full, self.n_rows, self.edges, self.ils,
          self.max_degree, self.rv, self.qm, self.core_terms, self.map_is_offset, self.n_entries, _) = (
             int(x) for x in info)
+        if demapper not in ("max_log", "exact"):
+            raise ComrsError(-1, f"demapper must be 'max_log' or 'exact', got {demapper!r}")
+        _check(lib().cb_code_set_demapper(h, int(demapper == "exact")), h)
+        self.demapper = demapper
         self.precision = precision
         self.dtype = np.float64 if precision == "f64" else np.float32
         self.rule, self.alpha, self.max_iterations = rule_l, alpha, max_iterations

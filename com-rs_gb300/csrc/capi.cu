@@ -65,6 +65,7 @@ struct cb_code {
   std::map<int, GenCache> gen;
   bool dev_ready = false;
   std::string err;
+  int exact_demap = 0;  // the frame generator's demapper: 1 exact, 0 max-log
   // the sum-product rule and the flooding schedule: the generic decoder on the lifted rows
   cb_ldpc* generic = nullptr;
   void* d_full = nullptr;
@@ -213,6 +214,7 @@ cb_status gen_device(cb_code* c, GenCache* g, uint64_t seed, uint64_t name_hash,
   a.ebn0_frames = ebn0_frames;
   a.b_bits = b;
   a.cw_out = cw_out;
+  a.exact = c->exact_demap;
   CB_CUDA(c, cbk::launch_gen<T>(a, s));
   return CB_OK;
 }
@@ -427,6 +429,14 @@ void cb_code_destroy(cb_code* c) {
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+cb_status cb_code_set_demapper(cb_code* c, int32_t exact) {
+  if (!c) return fail(nullptr, CB_ERR_CONFIG, "NULL code");
+  if (exact != 0 && exact != 1) return fail(c, CB_ERR_CONFIG, "demapper: 0 (max-log) or 1 (exact)");
+  std::lock_guard<std::mutex> lock(c->mu);
+  c->exact_demap = exact;
+  return CB_OK;
 }
 
 cb_status cb_code_info(const cb_code* c, int64_t info[16]) {

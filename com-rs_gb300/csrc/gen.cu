@@ -23,7 +23,8 @@
 //   symbols summed in symbol order, blocks/frame.rs:256-259);
 //   y = x + sqrt(sigma^2) * CN(0, 1)  (awgn.rs:94-99);
 //   L_b = max_{i: b=0} metric_i - max_{i: b=1} metric_i, metric_i = -|y - x_i|^2 /
-//   sigma^2 - ln M  (crates/com-mapping/src/demapper.rs:82-146, :270-297).
+//   sigma^2 - ln M  (crates/com-mapping/src/demapper.rs:82-146, :270-297), or with the
+//   exact demapper the log-sum-exp of each half of the labels.
 // f64 frames compute all of it in f64 with the correctly-rounded log/sin/cos of
 // crmath.cuh: bit-identical to the reference's draws up to the platform libm's last
 // bit.  f32 frames draw the same bits and the same uniforms, take the Gaussian in f32
@@ -207,7 +208,21 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
           if ((i >> shift) & 1) m1 = fmax(m1, met);
           else m0 = fmax(m0, met);
         }
-        out[t] = (T)__dsub_rn(m0, m1);
+        if (a.exact && isfinite(m0) && isfinite(m1)) {
+          // LabelHalves (demapper.rs:82-133): sums of exp(metric - max) in label order,
+          // L = m0 + ln s0 - m1 - ln s1; CUDA's exp and log where the reference calls libm
+          double s0 = 0.0, s1 = 0.0;
+          for (int i = 0; i < a.m; i++) {
+            double dr = __dsub_rn(yre, pts[2 * i]), di = __dsub_rn(yim, pts[2 * i + 1]);
+            double ns = __dadd_rn(__dmul_rn(dr, dr), __dmul_rn(di, di));
+            double met = __dadd_rn(__ddiv_rn(-ns, sigma2), uniform);
+            if ((i >> shift) & 1) s1 = __dadd_rn(s1, exp(__dsub_rn(met, m1)));
+            else s0 = __dadd_rn(s0, exp(__dsub_rn(met, m0)));
+          }
+          out[t] = (T)__dsub_rn(__dsub_rn(__dadd_rn(m0, log(s0)), m1), log(s1));
+        } else {
+          out[t] = (T)__dsub_rn(m0, m1);
+        }
       }
     }
   } else {
@@ -248,7 +263,21 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
           if ((lbl >> bitpos) & 1) m1 = fmaxf(m1, met);
           else m0 = fmaxf(m0, met);
         }
-        out[t] = (T)(m0 - m1);
+        if (a.exact) {
+          // exact log-sum-exp per dimension: the other dimension's sum is common to
+          // both halves of the labels and cancels
+          float s0 = 0.f, s1 = 0.f;
+          for (int q = 0; q < side; q++) {
+            int lbl = upper ? gray(side - 1 - q) : gray(q);
+            float dd = y - (upper ? lev_im[q] : lev_re[q]);
+            float met = -(dd * dd) * inv_s2;
+            if ((lbl >> bitpos) & 1) s1 += expf(met - m1);
+            else s0 += expf(met - m0);
+          }
+          out[t] = (T)(m0 + logf(s0) - m1 - logf(s1));
+        } else {
+          out[t] = (T)(m0 - m1);
+        }
       }
     }
   }
@@ -280,6 +309,7 @@ __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs
   g.llr_out = a.llr_out + (size_t)frame * c.e;
   g.info_out = a.info_out + (size_t)frame * ((c.k_info + 31) >> 5);
   g.cw_out = a.cw_out ? a.cw_out + (size_t)frame * ((c.n_full + 31) >> 5) : nullptr;
+  g.exact = a.exact;
   gen_one<T>(c, g, smem);
 }
 
@@ -309,6 +339,7 @@ __global__ void __launch_bounds__(NT) gen_mix_kernel(const __grid_constant__ Gen
   g.llr_out = a.llr + it.llr_offset;
   g.info_out = a.info + it.info_offset;
   g.cw_out = nullptr;
+  g.exact = 0;
   gen_one<float>(c, g, smem);
 }
 }  // namespace

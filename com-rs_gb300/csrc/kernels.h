@@ -52,6 +52,7 @@ struct GenArgs {
   const float* ebn0_frames = nullptr;
   double b_bits = 0.0;
   uint32_t* cw_out = nullptr;
+  int32_t exact = 0;           // demapper: 1 Jacobian::Exact (log-sum-exp), 0 max-log
 };
 constexpr int kGenThreads = 128;
 
@@ -66,6 +67,7 @@ struct GenFrame {
   T* llr_out;          // this frame's E LLRs
   uint32_t* info_out;  // its packed info bits
   uint32_t* cw_out;    // its packed codeword (optional)
+  int32_t exact;       // demapper: 1 exact (log-sum-exp), 0 max-log
 };
 
 // ---- mixed batches (mix.cu, gen.cu): codewords of different codes in one launch

@@ -79,6 +79,13 @@ void cb_code_destroy(cb_code* code);
 /* The message of the last error of `code` (or of the calling thread when NULL). */
 const char* cb_last_error(const cb_code* code);
 
+/* The demapper of the frame generator (cb_run_frames, cb_generate_frames and the
+ * learned decoder's training frames): 0 max-log (the default), 1 exact, the log-sum-exp
+ * of each half of the labels (Jacobian::MaxLog / Jacobian::Exact of
+ * crates/com-mapping/src/demapper.rs:82-146).  The exact demapper calls CUDA's exp and
+ * log where the reference calls the platform libm. */
+cb_status cb_code_set_demapper(cb_code* code, int32_t exact);
+
 /* info[0..16): base graph, Z, K', E, K (systematic columns), n_full, lifted rows,
  * edges, iLS, max row degree, rv, qm, core-inverse terms, 1 if the rate matching is
  * the plain offset 2Z + t, 0, 0. */

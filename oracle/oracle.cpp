@@ -155,6 +155,7 @@ struct Code {
   double alpha = 0.8;
   bool layered = true;
   int max_iterations = 50;
+  bool exact_demap = false;  // the trial's demapper: Jacobian::Exact, else MaxLog
   // NrLdpc part (nr/ldpc.rs:65-75)
   bool nr = false;
   int bg = 0, z = 0, ils = 0, k_info = 0, e = 0;
@@ -457,6 +458,36 @@ static bool qam_new(int m, Qam& q) {
 }
 
 // llr_kernel + llr_from_metrics + LabelHalves, max-log (demapper.rs:82-146, :270-297)
+// Jacobian::Exact (demapper.rs:82-133): per half of the labels, the largest metric and
+// the sum of exp(metric - max) in label order; L = m0 + ln s0 - m1 - ln s1
+static void demap_exact(const Qam& q, double yre, double yim, double sigma2, double* out) {
+  double metric[256];
+  double uniform = -q.log_m;
+  for (int i = 0; i < q.m; i++) {
+    double dr = yre - q.re[i], di = yim - q.im[i];
+    double ns = dr * dr + di * di;
+    metric[i] = -ns / sigma2 + uniform;
+  }
+  for (int o = 0; o < q.bits; o++) {
+    int shift = q.bits - 1 - o;
+    double m0 = -std::numeric_limits<double>::infinity(), m1 = m0;
+    for (int i = 0; i < q.m; i++) {
+      if (((i >> shift) & 1) == 0) m0 = std::fmax(m0, metric[i]);
+      else m1 = std::fmax(m1, metric[i]);
+    }
+    if (!std::isfinite(m0) || !std::isfinite(m1)) {
+      out[o] = m0 - m1;
+      continue;
+    }
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = 0; i < q.m; i++) {
+      if (((i >> shift) & 1) == 0) s0 += std::exp(metric[i] - m0);
+      else s1 += std::exp(metric[i] - m1);
+    }
+    out[o] = m0 + std::log(s0) - m1 - std::log(s1);
+  }
+}
+
 static void demap_maxlog(const Qam& q, double yre, double yim, double sigma2, double* out) {
   double metric[256];
   double uniform = -q.log_m;
@@ -520,7 +551,10 @@ static FrameResult run_trial(const Code& c, const Qam& q, Rng& rng, double ebn0_
     xi[s] += ni * sd;
   }
   std::vector<double> llr((size_t)ns * mb);
-  for (int s = 0; s < ns; s++) demap_maxlog(q, xr[s], xi[s], sigma2, &llr[(size_t)s * mb]);
+  for (int s = 0; s < ns; s++) {
+    if (c.exact_demap) demap_exact(q, xr[s], xi[s], sigma2, &llr[(size_t)s * mb]);
+    else demap_maxlog(q, xr[s], xi[s], sigma2, &llr[(size_t)s * mb]);
+  }
   // fec_decode reads the first E LLRs of the stream (the padding bits are dropped)
   std::vector<uint8_t> dec(kk);
   int it;
@@ -902,6 +936,12 @@ int or_qam_points(int m, double* re, double* im, double* log_m) {
   return 0;
 }
 
+void or_code_set_demapper(void* h, int exact) { ((Code*)h)->exact_demap = exact != 0; }
+void or_demap_exact(int m, const double* yre, const double* yim, int64_t n, double sigma2, double* out) {
+  Qam q;
+  if (!qam_new(m, q)) return;
+  for (int64_t s = 0; s < n; s++) demap_exact(q, yre[s], yim[s], sigma2, out + s * q.bits);
+}
 void or_demap_maxlog(int m, const double* yre, const double* yim, int64_t n, double sigma2, double* out) {
   Qam q;
   qam_new(m, q);

@@ -55,6 +55,8 @@ def lib():
         L.or_is_codeword.restype = i32
         L.or_is_codeword.argtypes = [vp, vp]
         L.or_bpsk_llr_batch.argtypes = [vp, u64, u64, u64, u64, i64, dbl, i32, vp, vp]
+        L.or_code_set_demapper.argtypes = [vp, i32]
+        L.or_demap_exact.argtypes = [i32, vp, vp, i64, dbl, vp]
         for f in (L.or_decode_f64, L.or_decode_f32):
             f.restype = i32
             f.argtypes = [vp, vp, vp, vp, vp]
@@ -118,6 +120,14 @@ def demap_maxlog(m, y, sigma2):
     return out
 
 
+def demap_exact(m, y, sigma2):
+    y = np.ascontiguousarray(y, np.complex128)
+    yr, yi = np.ascontiguousarray(y.real), np.ascontiguousarray(y.imag)
+    out = np.zeros(len(y) * (m.bit_length() - 1))
+    lib().or_demap_exact(m, _p(yr), _p(yi), len(y), sigma2, _p(out))
+    return out
+
+
 class Code:
     """The oracle's NrLdpc (or a generic LdpcCode read from an alist text)."""
 
@@ -138,6 +148,10 @@ class Code:
         if getattr(self, "h", None):
             lib().or_code_free(self.h)
             self.h = None
+
+    def set_demapper(self, exact):
+        lib().or_code_set_demapper(self.h, int(bool(exact)))
+        return self
 
     def set_decoder(self, rule=RULE_NMS, alpha=0.75, layered=True, max_iterations=20):
         lib().or_code_set_decoder(self.h, rule, alpha, int(layered), max_iterations)

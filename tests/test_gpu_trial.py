@@ -120,3 +120,42 @@ def test_campaign_counts_match_the_frames(cb, O):
         want = r.run_frames(4, 7, O.fnv1a64(NAME), c, 0, res[c].trials, eb, 0, O.NOISE_CR, 0)
         assert res[c].record["fer"].errors == int(want["frame_error"].sum())
         assert res[c].record["ber"].errors == int(want["bit_errors"].sum())
+
+
+@pytest.mark.parametrize("spec", [CODES[1], CODES[3], CODES[5]], ids=lambda s: f"k{s['k']}_m{s['m']}")
+def test_exact_demapper_f64_llrs_equal_the_oracle_to_rounding(cb, O, spec):
+    # Jacobian::Exact: the GPU calls CUDA's exp/log where the oracle calls libm, so the
+    # LLRs agree to a few ulps, and the bits and noise draws stay identical
+    g = cb.NrLdpc(spec["k"], spec["e"], base_graph=spec.get("bg"), lifting_size=spec.get("z"), precision="f64",
+                  demapper="exact")
+    r = O.Code(spec["k"], spec["e"], bg=spec.get("bg", 0), z=spec.get("z", 0)).set_decoder(O.RULE_NMS, 0.75, True, 20)
+    r.set_demapper(True)
+    n = 2 if spec["k"] > 4000 else 6
+    llr, info = g.generate_frames(7, NAME, 4, 0, n, 1.5, spec["m"])
+    ml, _ = cb.NrLdpc(spec["k"], spec["e"], base_graph=spec.get("bg"), lifting_size=spec.get("z"),
+                      precision="f64").generate_frames(7, NAME, 4, 0, n, 1.5, spec["m"])
+    for f in range(n):
+        rinfo, rllr, _ = r.trial(spec["m"], 7, O.fnv1a64(NAME), 4, f, 1.5, 0, O.NOISE_CR)
+        assert np.array_equal(info[f], rinfo)
+        assert np.allclose(llr[f], rllr, rtol=1e-13, atol=1e-13), np.max(np.abs(llr[f] - rllr))
+    assert not np.allclose(llr, ml)  # the exact LLRs are not the max-log ones
+
+
+def test_exact_demapper_f32_is_close_to_f64_and_decodes_alike(cb, O):
+    from conftest import load_package
+
+    ErrorRate = load_package().campaign.ErrorRate
+    spec = CODES[4]
+    kw = dict(base_graph=1, lifting_size=384, demapper="exact")
+    g32 = cb.NrLdpc(spec["k"], spec["e"], precision="f32", **kw)
+    g64 = cb.NrLdpc(spec["k"], spec["e"], precision="f64", **kw)
+    l32, i32 = g32.generate_frames(7, NAME, 0, 0, 4, 1.0, 16)
+    l64, i64 = g64.generate_frames(7, NAME, 0, 0, 4, 1.0, 16)
+    assert np.array_equal(i32, i64)
+    err = np.abs(l32.astype(np.float64) - l64) / np.maximum(np.abs(l64), 1.0)
+    assert np.median(err) < 1e-5 and np.mean(np.sign(l32) == np.sign(l64)) > 0.9999
+    # near the waterfall (about 2.5 dB) the two precisions give the same FER
+    a = g32.run_frames(7, NAME, 1, 0, 2048, 2.4, 16)["frame_error"].sum()
+    b = g64.run_frames(7, NAME, 1, 0, 2048, 2.4, 16)["frame_error"].sum()
+    (lo_a, hi_a), (lo_b, hi_b) = ErrorRate(int(a), 2048).wilson(0.99), ErrorRate(int(b), 2048).wilson(0.99)
+    assert not (hi_a < lo_b or hi_b < lo_a), (a, b)

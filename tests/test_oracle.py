@@ -175,3 +175,28 @@ def test_aff3ct_layered_nms_curve(O):
         assert not (a_hi < c_lo or c_hi < a_lo), (p["ebn0_db"], ours.rate(), theirs.rate())
         checked += 1
     assert checked >= 4
+
+
+@pytest.mark.parametrize("m", [4, 16, 64, 256])
+def test_exact_demapper_is_the_log_sum_exp_of_the_label_halves(O, m):
+    # Jacobian::Exact (crates/com-mapping/src/demapper.rs:82-133) against an independent
+    # log-sum-exp over the two halves of the labels, MSB first
+    pts, log_m = O.qam(m)
+    rng = np.random.default_rng(m)
+    y = pts[rng.integers(0, m, 200)] + 0.3 * (rng.standard_normal(200) + 1j * rng.standard_normal(200))
+    sigma2 = 0.18
+    got = O.demap_exact(m, y, sigma2).reshape(200, -1)
+    b = m.bit_length() - 1
+    metric = -np.abs(y[:, None] - pts[None, :]) ** 2 / sigma2 - log_m
+    labels = np.arange(m)
+    for o in range(b):
+        half = (labels >> (b - 1 - o)) & 1
+        want = np.logaddexp.reduce(metric[:, half == 0], axis=1) - np.logaddexp.reduce(metric[:, half == 1], axis=1)
+        assert np.allclose(got[:, o], want, rtol=1e-12, atol=1e-12)
+    # max-log keeps the largest term only: the exact LLR is smaller in magnitude near
+    # the decision boundary and equal in sign far from it; QPSK has one point per half
+    ml = O.demap_maxlog(m, y, sigma2).reshape(200, -1)
+    if m == 4:
+        assert np.allclose(got, ml, rtol=1e-13, atol=1e-13)
+    else:
+        assert not np.allclose(got, ml)
