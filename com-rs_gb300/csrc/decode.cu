@@ -111,11 +111,12 @@ __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(co
         // the state of a layer is prefetched one layer ahead
         T a1 = (T)0, a2 = (T)0;
         uint32_t mt = 0;
-        if (iter > 1 && active) st.load(tid, a1, a2, mt);
-        for (int L = 0; L < c.rows_n; L++) {
+        if (iter > 1 && active) st.load(c.layer_order[0] * z + tid, a1, a2, mt);
+        for (int q = 0; q < c.rows_n; q++) {
+          const int L = c.layer_order[q];
           T p1 = (T)0, p2 = (T)0;
           uint32_t pm = 0;
-          if (iter > 1 && active && L + 1 < c.rows_n) st.load((L + 1) * z + tid, p1, p2, pm);
+          if (iter > 1 && active && q + 1 < c.rows_n) st.load(c.layer_order[q + 1] * z + tid, p1, p2, pm);
           if (active) {
             const int s0 = c.layer_start[L];
             const int d = c.layer_start[L + 1] - s0;
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(co
           a1 = p1;
           a2 = p2;
           mt = pm;
-          __syncthreads();
+          if ((c.level_break >> q) & 1ull) __syncthreads();
         }
         if (!some_check_fails(post, hd, s_ent, s_lstart, c.rows_n, ncol, z, tid, nt)) {
           it = iter;
