@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(co
           a1 = p1;
           a2 = p2;
           mt = pm;
-          if ((c.level_break >> q) & 1ull) __syncthreads();
+          if (c.level_end[q]) __syncthreads();
         }
         if (!some_check_fails(post, hd, s_ent, s_lstart, c.rows_n, ncol, z, tid, nt)) {
           it = iter;

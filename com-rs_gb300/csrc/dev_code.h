@@ -46,11 +46,10 @@ inline void fill_dev_code(const cbh::NrCode& h, cbd::DevCode& v) {
       levels = std::max(levels, lv + 1);
     }
     int pos = 0;
-    v.level_break = 0;
     for (int lv = 0; lv < levels; lv++) {
       for (int L = 0; L < h.rows_n; L++)
         if (level[L] == lv) v.layer_order[pos++] = (uint8_t)L;
-      v.level_break |= 1ull << (pos - 1);
+      v.level_end[pos - 1] = 1;
     }
   }
   for (int t = 0; t < v.n_core_terms; t++)

@@ -97,10 +97,10 @@ struct DevCode {
   uint32_t core_term[cbh::kMaxCoreTerms];  // (block << 20) | (src << 16) | shift
   uint2 eaddr[cbh::kMaxEntries];           // {4 (column Z + shift), Z - shift}
   // the layered schedule by levels: the layers in the order the decoder runs them, and a
-  // bit per position set when a barrier follows it (layers between two barriers share
+  // flag per position set when a barrier follows it (layers between two barriers share
   // no column, so their lifted rows run at once with the sequential order's results)
   uint8_t layer_order[cbh::kMaxLayers];
-  uint64_t level_break;
+  uint8_t level_end[cbh::kMaxLayers];
 };
 
 // decoder settings (crates/com-fec/src/ldpc.rs:165-172)
