@@ -41,13 +41,13 @@ SEED, NAME = 7, "bicm_ldpc_c2"
 # algorithmic bytes of one decoded codeword: E f32 LLRs in, ceil(K'/8) decision bytes out,
 # a 4-byte record (iteration count)
 ALGO_BYTES = E * 4 + (K_INFO + 7) // 8 + 4
-# DRAM bytes (read + write) of the decoder per codeword at 20 iterations, from one ncu capture
-# of a 2048-codeword launch (profiles/decode_c2_f32_dram.md: 412,941,056 + 2,174,569,216 B);
-# the persistent grid keeps the same 304 state slots at any batch, so it scales by codewords
-DRAM_BYTES_PER_CODEWORD = (412_941_056 + 2_174_569_216) / 2048
-# warp-instructions the decoder issues per codeword and iteration, from the same kind of
-# capture (smsp__inst_executed.sum = 5,044,612,288 for 2048 codewords x 20 iterations)
-WARP_INST_PER_CODEWORD_ITERATION = 5_044_612_288 / (2048 * 20)
+# DRAM bytes (read + write) of the decoder per codeword at 20 iterations, and the
+# warp-instructions it issues per codeword and iteration, from one ncu capture of a
+# 2048-codeword launch (profiles/decode_c2_f32.md: 547,636,224 + 2,582,025,216 B,
+# smsp__inst_executed.sum = 4,976,807,104); the persistent grid keeps the same 304 state
+# slots at any batch, so both scale by codewords
+DRAM_BYTES_PER_CODEWORD = (547_636_224 + 2_582_025_216) / 2048
+WARP_INST_PER_CODEWORD_ITERATION = 4_976_807_104 / (2048 * 20)
 WORKLOAD = ("5G NR LDPC BG1 Z=384 K'=8448 E=25344 (rate 1/3), Gray 16-QAM, AWGN Eb/N0 0:0.25:2 dB, "
             "max-log LLRs, layered NMS alpha=0.75, <=20 iterations + syndrome stop, f32, 8192 codewords/launch")
 
