@@ -77,6 +77,7 @@ SYMBOLS = [
     ("cb_nms_forward", _i32, [_vp, _vp, _i64, _vp]),
     ("cb_nms_gradients", _i32, [_vp, _vp, _vp, _i64, _i32, _vp, _vp, C.POINTER(_dbl)]),
     ("cb_nms_train_step", _i32, [_vp, _i32, _u64, _u64, _i64, _dbl, _dbl, _dbl, _i32, C.POINTER(_dbl)]),
+    ("cb_nms_decode", _i32, [_vp, _vp, _i64, _vp, _vp]),
     ("cb_nms_run_frames", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp]),
     ("cb_mix_create", _i32, [_vp, _i64, _u64, _u64, _dbl, _i32, _i32, C.POINTER(_vp)]),
     ("cb_mix_destroy", None, [_vp]),
@@ -323,6 +324,14 @@ class LearnedNms:
         post = np.zeros((x.shape[0], self.code.n_full), np.float32)
         _check(lib().cb_nms_forward(self._h, _p(x), x.shape[0], _p(post)), self.code._h)
         return post
+
+    def decode(self, llr):
+        """(posteriors [n x n_full], iterations) with the syndrome stop after each iteration."""
+        x = np.ascontiguousarray(llr, np.float32).reshape(-1, self.code.e)
+        post = np.zeros((x.shape[0], self.code.n_full), np.float32)
+        its = np.zeros(x.shape[0], np.int32)
+        _check(lib().cb_nms_decode(self._h, _p(x), x.shape[0], _p(post), _p(its)), self.code._h)
+        return post, its
 
     def gradients(self, llr, cw, multi_loss=False):
         x = np.ascontiguousarray(llr, np.float32).reshape(-1, self.code.e)

@@ -645,6 +645,34 @@ cb_status nms_buffers(cb_nms* h, int64_t n, bool train) {
   return CB_OK;
 }
 
+// evaluation of the learned min-sum: the layered decoder with the network's weights and
+// the syndrome stop (the same results as the training forward with an early stop)
+cb_status nms_eval(cb_nms* h, const float* llr, int64_t n, const uint32_t* ref, cbd::FrameResult* results,
+                   float* post, int32_t* iters, cudaStream_t s) {
+  cb_code* c = h->code;
+  cbk::DecodeArgs<float> a;
+  a.code = c->dev;
+  a.cfg = c->cfg;
+  a.cfg.max_iterations = h->T;
+  a.llr = llr;
+  a.n_frames = n;
+  a.bits_out = nullptr;
+  a.app_out = nullptr;
+  a.post_out = post;
+  a.iters_out = iters;
+  a.ref_bits = ref;
+  a.results = results;
+  a.state = reinterpret_cast<float*>(c->d_state);
+  a.work_counter = reinterpret_cast<int32_t*>(c->d_counter);
+  a.status = c->d_status;
+  a.l_alpha = h->d_w;
+  a.l_beta = h->d_w + h->nw;
+  a.l_shared = h->shared;
+  CB_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), s));
+  CB_CUDA(c, cbk::launch_decode<float>(a, (int)std::min<int64_t>(c->decode_grid, n), s));
+  return CB_OK;
+}
+
 cbk::LearnedArgs nms_args(cb_nms* h, int64_t n) {
   cbk::LearnedArgs a{};
   a.code = h->code->dev;
@@ -826,6 +854,31 @@ cb_status cb_nms_train_step(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_h
   return CB_OK;
 }
 
+cb_status cb_nms_decode(cb_nms* h, const float* llr, int64_t n, float* post, int32_t* iterations) {
+  if (!h || (!llr && n > 0) || n < 0) return fail(nullptr, CB_ERR_CONFIG, "NULL argument or negative count");
+  cb_code* c = h->code;
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (n == 0) return CB_OK;
+  const int64_t chunk = 16384;
+  for (int64_t done = 0; done < n; done += chunk) {
+    const int64_t cnt = std::min(chunk, n - done);
+    if (cb_status st = nms_buffers(h, cnt, false)) return st;
+    CB_CUDA(c, grow(c->d_iters, c->iters_cap, (size_t)cnt * 4));
+    CB_CUDA(c, cudaMemcpyAsync(h->d_llr, llr + (size_t)done * c->host.e, (size_t)cnt * c->host.e * 4,
+                               cudaMemcpyHostToDevice, c->stream));
+    if (cb_status st = nms_eval(h, h->d_llr, cnt, nullptr, nullptr, post ? h->d_post : nullptr, c->d_iters, c->stream))
+      return st;
+    if (post)
+      CB_CUDA(c, cudaMemcpyAsync(post + (size_t)done * c->host.n_full, h->d_post, (size_t)cnt * c->host.n_full * 4,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    if (iterations)
+      CB_CUDA(c, cudaMemcpyAsync(iterations + done, c->d_iters, (size_t)cnt * 4, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CB_OK;
+}
+
 cb_status cb_nms_run_frames(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first,
                             int64_t n, double ebn0_db, cb_frame_result* out) {
   if (!h || !out || n < 0) return fail(nullptr, CB_ERR_CONFIG, "NULL argument or negative count");
@@ -842,12 +895,7 @@ cb_status cb_nms_run_frames(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_h
     if (cb_status st = gen_device<float>(c, g, seed, name_hash, cond, first + done, cnt, ebn0_db, h->d_llr, h->d_info,
                                          c->stream))
       return st;
-    cbk::LearnedArgs a = nms_args(h, cnt);
-    a.early_stop = 1;
-    a.post_out = nullptr;
-    a.ref_bits = h->d_info;
-    a.results = h->d_res;
-    CB_CUDA(c, cbk::launch_learned(a, true, c->stream));
+    if (cb_status st = nms_eval(h, h->d_llr, cnt, h->d_info, h->d_res, nullptr, nullptr, c->stream)) return st;
     CB_CUDA(c, cudaMemcpyAsync(out + done, h->d_res, (size_t)cnt * sizeof(cb_frame_result), cudaMemcpyDeviceToHost,
                                c->stream));
   }

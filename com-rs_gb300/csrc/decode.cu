@@ -50,7 +50,8 @@ __host__ __device__ __forceinline__ size_t decode_smem_bytes(int n_full, int z, 
   return (b + 15) & ~(size_t)15;
 }
 
-template <typename T>
+// LEARNED (f32 only): the learned min-sum with per-edge, per-iteration weights
+template <typename T, bool LEARNED>
 __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(const __grid_constant__ DecodeArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const cbd::DevCode& c = a.code;
@@ -122,7 +123,11 @@ __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(co
             const int d = c.layer_start[L + 1] - s0;
             T n1, n2;
             uint32_t nm;
-            if constexpr (sizeof(T) == 4)
+            if constexpr (LEARNED)
+              row_dispatch_learned(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z},
+                                   LearnedRowW{a.l_alpha, a.l_beta, c.n_entries, z, a.l_shared, s0, tid}, iter - 1,
+                                   iter == 1, a1, a2, mt, n1, n2, nm);
+            else if constexpr (sizeof(T) == 4)
               row_dispatch_lean(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z}, a1, a2, mt, rule, alpha,
                                 n1, n2, nm);
             else
@@ -176,9 +181,10 @@ __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(co
 }
 
 template <typename T>
-void* kernel_for(int max_degree) {
-  (void)max_degree;
-  return (void*)layered_kernel<T>;
+void* kernel_for(bool learned) {
+  if constexpr (sizeof(T) == 4)
+    if (learned) return (void*)layered_kernel<T, true>;
+  return (void*)layered_kernel<T, false>;
 }
 
 int block_threads(int z) { return ((z + 31) / 32) * 32; }
@@ -196,7 +202,7 @@ size_t decode_state_bytes_per_slot(const cbd::DevCode& c, int precision) {
 }
 
 int decode_grid_size(const cbd::DevCode& c, int precision, int device) {
-  void* k = precision == 0 ? kernel_for<double>(c.max_degree) : kernel_for<float>(c.max_degree);
+  void* k = precision == 0 ? kernel_for<double>(false) : kernel_for<float>(false);
   size_t smem = smem_bytes(c, precision);
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 0, sms = 0;
@@ -208,7 +214,7 @@ int decode_grid_size(const cbd::DevCode& c, int precision, int device) {
 template <typename T>
 cudaError_t launch_decode(const DecodeArgs<T>& a, int grid, cudaStream_t stream) {
   const int precision = sizeof(T) == 8 ? 0 : 1;
-  void* k = kernel_for<T>(a.code.max_degree);
+  void* k = kernel_for<T>(a.l_alpha != nullptr);
   size_t smem = smem_bytes(a.code, precision);
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

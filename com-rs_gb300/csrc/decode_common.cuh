@@ -275,6 +275,89 @@ __device__ __forceinline__ void row_update_lean(float* __restrict__ post, const 
   nm = (sm << 8) | (uint32_t)i1;
 }
 
+// The learned min-sum's weights of one row: alpha and beta of (iteration t, entry s0 + e)
+// for lifted row r, shared by the Z rows or one per lifted edge.
+struct LearnedRowW {
+  const float* alpha;
+  const float* beta;
+  int n_entries, z, shared, s0, r;
+  __device__ __forceinline__ float magnitude(int t, int e, float m) const {
+    const size_t i = shared ? (size_t)t * n_entries + s0 + e : ((size_t)t * n_entries + s0 + e) * z + r;
+    const float am = __fsub_rn(__fmul_rn(__ldg(alpha + i), m), __ldg(beta + i));
+    return am > 0.f ? am : 0.f;
+  }
+};
+
+// One lifted row of the learned min-sum (the forward of nms_learned.cu, same results):
+// the state keeps the raw minimum and second minimum (the weights differ per edge), and
+// each edge's message magnitude is max(alpha m - beta, 0) with its own weights, the
+// previous iteration's for the old message.  `first`: no old messages yet.
+template <int D, typename Addr>
+__device__ __forceinline__ void row_update_learned(float* __restrict__ post, const Addr& addr, const LearnedRowW& w,
+                                                   int t, bool first, float a1, float a2, uint32_t mt, float& n1,
+                                                   float& n2, uint32_t& nm) {
+  int off[D];
+  float x[D];
+  const int old_i1 = (int)(mt & 31u);
+  const uint32_t t0 = mt << (24 - D);
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    off[e] = addr(e);
+    const float p = ld_post(post, off[e]);
+    if (first) {
+      x[e] = __fsub_rn(p, 0.f);
+    } else {
+      const float mag = w.magnitude(t - 1, e, (e == old_i1) ? a2 : a1);
+      x[e] = ((t0 << e) & 0x80000000u) ? __fadd_rn(p, mag) : __fsub_rn(p, mag);
+    }
+  }
+  float m1 = infinity<float>(), m2 = infinity<float>();
+#pragma unroll
+  for (int e = 0; e + 1 < D; e += 2) {
+    const float s = min_xorsign_abs(x[e], x[e + 1]);
+    const float l = fmaxf(fabsf(x[e]), fabsf(x[e + 1]));
+    m2 = min3f(m2, fmaxf(fabsf(m1), fabsf(s)), l);
+    m1 = min_xorsign_abs(m1, s);
+  }
+  if (D & 1) {
+    m2 = fminf(m2, fmaxf(fabsf(m1), fabsf(x[D - 1])));
+    m1 = min_xorsign_abs(m1, x[D - 1]);
+  }
+  const uint32_t ps = __float_as_uint(m1) & 0x80000000u;
+  m1 = fabsf(m1);
+  uint32_t sm = 0;
+  int i1 = 0;
+#pragma unroll
+  for (int e = 0; e < D; e++) {
+    const bool eq = fabsf(x[e]) == m1;
+    i1 = eq ? e : i1;
+    const float mag = w.magnitude(t, e, eq ? m2 : m1);
+    const uint32_t ob = __float_as_uint(mag) | ((ps ^ __float_as_uint(x[e])) & 0x80000000u);
+    st_post(post, off[e], __fadd_rn(x[e], __uint_as_float(ob)));
+    sm = (sm << 1) | (ob >> 31);
+  }
+  n1 = m1;
+  n2 = m2;
+  nm = (sm << 8) | (uint32_t)i1;
+}
+
+template <typename Addr>
+__device__ __forceinline__ void row_dispatch_learned(int d, float* post, const Addr& addr, const LearnedRowW& w, int t,
+                                                     bool first, float a1, float a2, uint32_t mt, float& n1,
+                                                     float& n2, uint32_t& nm) {
+  switch (d) {
+    case 3: row_update_learned<3>(post, addr, w, t, first, a1, a2, mt, n1, n2, nm); break;
+    case 4: row_update_learned<4>(post, addr, w, t, first, a1, a2, mt, n1, n2, nm); break;
+    case 5: row_update_learned<5>(post, addr, w, t, first, a1, a2, mt, n1, n2, nm); break;
+    case 6: row_update_learned<6>(post, addr, w, t, first, a1, a2, mt, n1, n2, nm); break;
+    case 7: row_update_learned<7>(post, addr, w, t, first, a1, a2, mt, n1, n2, nm); break;
+    case 8: row_update_learned<8>(post, addr, w, t, first, a1, a2, mt, n1, n2, nm); break;
+    case 9: row_update_learned<9>(post, addr, w, t, first, a1, a2, mt, n1, n2, nm); break;
+    case 10: row_update_learned<10>(post, addr, w, t, first, a1, a2, mt, n1, n2, nm); break;
+    default: row_update_learned<19>(post, addr, w, t, first, a1, a2, mt, n1, n2, nm); break;
+  }
+}
+
 template <typename Addr>
 __device__ __forceinline__ void row_dispatch_lean(int d, float* post, const Addr& addr, float a1, float a2,
                                                   uint32_t mt, int rule, float alpha, float& n1, float& n2,

@@ -24,6 +24,11 @@ struct DecodeArgs {
   T* state;                 // check-node state, state_bytes_per_slot() per resident CTA
   int32_t* work_counter;    // zeroed before the launch
   int32_t* status;          // error word (0 = ok)
+  // learned min-sum (f32): the check message of iteration t, edge e is
+  // s max(alpha[t,e] m - beta[t,e], 0); weights [t][entry] (shared) or [t][entry][r]
+  const float* l_alpha = nullptr;
+  const float* l_beta = nullptr;
+  int32_t l_shared = 0;
 };
 
 // the number of resident CTAs the persistent decoder launches and the state each needs

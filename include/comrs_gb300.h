@@ -168,6 +168,11 @@ cb_status cb_nms_gradients(cb_nms* nms, const float* llr, const uint8_t* cw, int
 cb_status cb_nms_train_step(cb_nms* nms, int32_t modulation_order, uint64_t seed, uint64_t name_hash,
                             int64_t batch, double ebn0_lo, double ebn0_hi, double lr, int32_t multi_loss,
                             double* loss);
+/* decode n frames of E LLRs (host) with the learned decoder and the syndrome stop after
+ * each iteration: the n_full posteriors (nullable) and the iterations used (nullable).
+ * Runs the layered decoder with the network's weights (the same results as the
+ * training forward, which runs all iterations) */
+cb_status cb_nms_decode(cb_nms* nms, const float* llr, int64_t n_frames, float* post, int32_t* iterations);
 /* cb_run_frames with the learned decoder (syndrome stop after each iteration) */
 cb_status cb_nms_run_frames(cb_nms* nms, int32_t modulation_order, uint64_t seed, uint64_t name_hash,
                             uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,

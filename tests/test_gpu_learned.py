@@ -75,3 +75,32 @@ def test_training_gains_over_the_plain_min_sum(cb):
     learned = net.run_frames(13, "c4_eval", 0, 0, n, eb, 4)
     fp, fl = int(plain["frame_error"].sum()), int(learned["frame_error"].sum())
     assert fp > 500 and fl < 0.7 * fp, (fl, fp)
+
+
+@pytest.mark.parametrize("shared", [False, True])
+def test_fast_evaluation_equals_the_training_forward(cb, O, shared):
+    # the layered decoder with the network's weights (cb_nms_decode, cb_nms_run_frames)
+    # against the training forward (all T iterations, no stop): equal posteriors on every
+    # frame that runs all T iterations; the others stop on a codeword
+    T = 8
+    g = cb.NrLdpc(520, 1040, base_graph=2, lifting_size=52, precision="f32", max_iterations=T)
+    net = cb.LearnedNms(g, T, shared=shared)
+    rng = np.random.default_rng(7)
+    net.set_weights((0.8 + 0.1 * rng.standard_normal(net.n_weights)).astype(np.float32),
+                    (0.1 * rng.standard_normal(net.n_weights)).astype(np.float32))
+    ref = O.Code(520, 1040, bg=2, z=52)
+    llr, _ = oracle_frames(O, ref, 64, 1.0)
+    post, its = net.decode(llr)
+    full = net.forward(llr)
+    ran_all = its == T
+    assert ran_all.sum() >= 8 and (~ran_all).sum() >= 8
+    assert np.array_equal(post[ran_all].view(np.uint32), full[ran_all].view(np.uint32))
+    for f in np.flatnonzero(~ran_all):
+        assert ref.is_codeword((post[f] < 0).astype(np.uint8))
+    # the Monte Carlo records come from the same path
+    rec = net.run_frames(5, NAME, 0, 0, 64, 1.0, 4)
+    llr2, info2 = g.generate_frames(5, NAME, 0, 0, 64, 1.0, 4)
+    post2, its2 = net.decode(llr2)
+    assert np.array_equal(rec["iterations"], its2)
+    errs = ((post2[:, :520] < 0) != info2.astype(bool)).sum(axis=1)
+    assert np.array_equal(rec["bit_errors"], errs)
