@@ -645,10 +645,25 @@ cb_status nms_buffers(cb_nms* h, int64_t n, bool train) {
   return CB_OK;
 }
 
+// Whether the network's weights go in the launch parameters: shared, small enough, and a
+// large lifting.  With Z >= 128 few CTAs share an SM and the weights stay in the constant
+// cache (BG1 Z = 384: 3.9 against 3.2 Gbit/s from global memory); with small Z a dozen
+// CTAs at different iterations thrash it (BG2 Z = 52: 1.6 against 1.9 Gbit/s).  Then `w`
+// receives a host copy of the weights (scales then offsets).
+cb_status nms_param_weights(cb_nms* h, std::vector<float>& w, bool& in_params) {
+  cb_code* c = h->code;
+  in_params = h->shared && h->nw <= cbk::kMaxParamWeights && c->dev.z >= 128;
+  if (!in_params) return CB_OK;
+  w.resize((size_t)2 * h->nw);
+  CB_CUDA(c, cudaMemcpyAsync(w.data(), h->d_w, w.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+  CB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CB_OK;
+}
+
 // evaluation of the learned min-sum: the layered decoder with the network's weights and
 // the syndrome stop (the same results as the training forward with an early stop)
 cb_status nms_eval(cb_nms* h, const float* llr, int64_t n, const uint32_t* ref, cbd::FrameResult* results,
-                   float* post, int32_t* iters, cudaStream_t s) {
+                   float* post, int32_t* iters, cudaStream_t s, const std::vector<float>* param_w) {
   cb_code* c = h->code;
   cbk::DecodeArgs<float> a;
   a.code = c->dev;
@@ -669,7 +684,17 @@ cb_status nms_eval(cb_nms* h, const float* llr, int64_t n, const uint32_t* ref, 
   a.l_beta = h->d_w + h->nw;
   a.l_shared = h->shared;
   CB_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), s));
-  CB_CUDA(c, cbk::launch_decode<float>(a, (int)std::min<int64_t>(c->decode_grid, n), s));
+  const int grid = (int)std::min<int64_t>(c->decode_grid, n);
+  if (param_w) {
+    // ~30 KB of launch parameters: built once per call site, copied by the launch
+    static thread_local cbk::LearnedParamArgs pa;
+    pa.d = a;
+    std::memcpy(pa.alpha, param_w->data(), (size_t)h->nw * 4);
+    std::memcpy(pa.beta, param_w->data() + h->nw, (size_t)h->nw * 4);
+    CB_CUDA(c, cbk::launch_decode_learned_param(pa, grid, s));
+  } else {
+    CB_CUDA(c, cbk::launch_decode<float>(a, grid, s));
+  }
   return CB_OK;
 }
 
@@ -860,6 +885,9 @@ cb_status cb_nms_decode(cb_nms* h, const float* llr, int64_t n, float* post, int
   std::lock_guard<std::mutex> lock(c->mu);
   CB_CUDA(c, cudaSetDevice(c->device));
   if (n == 0) return CB_OK;
+  std::vector<float> pw;
+  bool in_params = false;
+  if (cb_status st = nms_param_weights(h, pw, in_params)) return st;
   const int64_t chunk = 16384;
   for (int64_t done = 0; done < n; done += chunk) {
     const int64_t cnt = std::min(chunk, n - done);
@@ -867,7 +895,8 @@ cb_status cb_nms_decode(cb_nms* h, const float* llr, int64_t n, float* post, int
     CB_CUDA(c, grow(c->d_iters, c->iters_cap, (size_t)cnt * 4));
     CB_CUDA(c, cudaMemcpyAsync(h->d_llr, llr + (size_t)done * c->host.e, (size_t)cnt * c->host.e * 4,
                                cudaMemcpyHostToDevice, c->stream));
-    if (cb_status st = nms_eval(h, h->d_llr, cnt, nullptr, nullptr, post ? h->d_post : nullptr, c->d_iters, c->stream))
+    if (cb_status st = nms_eval(h, h->d_llr, cnt, nullptr, nullptr, post ? h->d_post : nullptr, c->d_iters, c->stream,
+                                in_params ? &pw : nullptr))
       return st;
     if (post)
       CB_CUDA(c, cudaMemcpyAsync(post + (size_t)done * c->host.n_full, h->d_post, (size_t)cnt * c->host.n_full * 4,
@@ -888,6 +917,9 @@ cb_status cb_nms_run_frames(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_h
   if (n == 0) return CB_OK;
   GenCache* g;
   if (cb_status st = gen_config(c, m, &g)) return st;
+  std::vector<float> pw;
+  bool in_params = false;
+  if (cb_status st = nms_param_weights(h, pw, in_params)) return st;
   const int64_t chunk = 16384;
   for (int64_t done = 0; done < n; done += chunk) {
     int64_t cnt = std::min(chunk, n - done);
@@ -895,7 +927,9 @@ cb_status cb_nms_run_frames(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_h
     if (cb_status st = gen_device<float>(c, g, seed, name_hash, cond, first + done, cnt, ebn0_db, h->d_llr, h->d_info,
                                          c->stream))
       return st;
-    if (cb_status st = nms_eval(h, h->d_llr, cnt, h->d_info, h->d_res, nullptr, nullptr, c->stream)) return st;
+    if (cb_status st = nms_eval(h, h->d_llr, cnt, h->d_info, h->d_res, nullptr, nullptr, c->stream,
+                                in_params ? &pw : nullptr))
+      return st;
     CB_CUDA(c, cudaMemcpyAsync(out + done, h->d_res, (size_t)cnt * sizeof(cb_frame_result), cudaMemcpyDeviceToHost,
                                c->stream));
   }

@@ -50,9 +50,9 @@ __host__ __device__ __forceinline__ size_t decode_smem_bytes(int n_full, int z, 
   return (b + 15) & ~(size_t)15;
 }
 
-// LEARNED (f32 only): the learned min-sum with per-edge, per-iteration weights
+// LEARNED (f32 only): the learned min-sum with per-edge, per-iteration weights la, lb
 template <typename T, bool LEARNED>
-__global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(const __grid_constant__ DecodeArgs<T> a) {
+__device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float* la, const float* lb) {
   extern __shared__ __align__(16) unsigned char smem[];
   const cbd::DevCode& c = a.code;
   const int z = c.z, nt = blockDim.x, tid = threadIdx.x;
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(co
             uint32_t nm;
             if constexpr (LEARNED)
               row_dispatch_learned(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z},
-                                   LearnedRowW{a.l_alpha, a.l_beta, c.n_entries, z, a.l_shared, s0, tid}, iter - 1,
+                                   LearnedRowW{la, lb, c.n_entries, z, a.l_shared, s0, tid}, iter - 1,
                                    iter == 1, a1, a2, mt, n1, n2, nm);
             else if constexpr (sizeof(T) == 4)
               row_dispatch_lean(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z}, a1, a2, mt, rule, alpha,
@@ -180,6 +180,15 @@ __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(co
   }
 }
 
+template <typename T, bool LEARNED>
+__global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(const __grid_constant__ DecodeArgs<T> a) {
+  decode_body<T, LEARNED>(a, a.l_alpha, a.l_beta);
+}
+
+__global__ void __launch_bounds__(384, 2) layered_learned_param_kernel(const __grid_constant__ LearnedParamArgs a) {
+  decode_body<float, true>(a.d, a.alpha, a.beta);
+}
+
 template <typename T>
 void* kernel_for(bool learned) {
   if constexpr (sizeof(T) == 4)
@@ -220,6 +229,15 @@ cudaError_t launch_decode(const DecodeArgs<T>& a, int grid, cudaStream_t stream)
   if (e != cudaSuccess) return e;
   void* args[] = {(void*)&a};
   return cudaLaunchKernel(k, dim3(grid), dim3(block_threads(a.code.z)), args, smem, stream);
+}
+
+cudaError_t launch_decode_learned_param(const LearnedParamArgs& a, int grid, cudaStream_t stream) {
+  void* k = (void*)layered_learned_param_kernel;
+  size_t smem = smem_bytes(a.d.code, 1);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {(void*)&a};
+  return cudaLaunchKernel(k, dim3(grid), dim3(block_threads(a.d.code.z)), args, smem, stream);
 }
 
 template cudaError_t launch_decode<double>(const DecodeArgs<double>&, int, cudaStream_t);

@@ -276,14 +276,15 @@ __device__ __forceinline__ void row_update_lean(float* __restrict__ post, const 
 }
 
 // The learned min-sum's weights of one row: alpha and beta of (iteration t, entry s0 + e)
-// for lifted row r, shared by the Z rows or one per lifted edge.
+// for lifted row r, shared by the Z rows or one per lifted edge (in global memory or in
+// the launch parameters).
 struct LearnedRowW {
   const float* alpha;
   const float* beta;
   int n_entries, z, shared, s0, r;
   __device__ __forceinline__ float magnitude(int t, int e, float m) const {
     const size_t i = shared ? (size_t)t * n_entries + s0 + e : ((size_t)t * n_entries + s0 + e) * z + r;
-    const float am = __fsub_rn(__fmul_rn(__ldg(alpha + i), m), __ldg(beta + i));
+    const float am = __fsub_rn(__fmul_rn(alpha[i], m), beta[i]);
     return am > 0.f ? am : 0.f;
   }
 };

@@ -31,6 +31,16 @@ struct DecodeArgs {
   int32_t l_shared = 0;
 };
 
+// The learned decoder with its weights in the launch parameters (weights shared across
+// Z, at most kMaxParamWeights per kind): warp-uniform reads through the constant cache.
+constexpr int kMaxParamWeights = 3200;
+struct LearnedParamArgs {
+  DecodeArgs<float> d;
+  float alpha[kMaxParamWeights];
+  float beta[kMaxParamWeights];
+};
+cudaError_t launch_decode_learned_param(const LearnedParamArgs& a, int grid, cudaStream_t stream);
+
 // the number of resident CTAs the persistent decoder launches and the state each needs
 int decode_grid_size(const cbd::DevCode& code, int precision, int device);
 size_t decode_state_bytes_per_slot(const cbd::DevCode& code, int precision);

@@ -89,7 +89,7 @@ def test_fast_evaluation_equals_the_training_forward(cb, O, shared):
     net.set_weights((0.8 + 0.1 * rng.standard_normal(net.n_weights)).astype(np.float32),
                     (0.1 * rng.standard_normal(net.n_weights)).astype(np.float32))
     ref = O.Code(520, 1040, bg=2, z=52)
-    llr, _ = oracle_frames(O, ref, 64, 1.0)
+    llr = np.concatenate([oracle_frames(O, ref, 32, eb)[0] for eb in (1.0, 3.0)])
     post, its = net.decode(llr)
     full = net.forward(llr)
     ran_all = its == T
