@@ -647,9 +647,10 @@ cb_status nms_buffers(cb_nms* h, int64_t n, bool train) {
 
 // Whether the network's weights go in the launch parameters: shared, small enough, and a
 // large lifting.  With Z >= 128 few CTAs share an SM and the weights stay in the constant
-// cache (BG1 Z = 384: 3.9 against 3.2 Gbit/s from global memory); with small Z a dozen
-// CTAs at different iterations thrash it (BG2 Z = 52: 1.6 against 1.9 Gbit/s).  Then `w`
-// receives a host copy of the weights (scales then offsets).
+// cache (BG1 Z = 384: 3.9 against 3.2 Gbit/s from global memory), and shared memory has
+// no room left beside the posteriors; with small Z a dozen CTAs at different iterations
+// thrash that cache, and each iteration's weights are staged in shared memory instead.
+// Then `w` receives a host copy of the weights (scales then offsets).
 cb_status nms_param_weights(cb_nms* h, std::vector<float>& w, bool& in_params) {
   cb_code* c = h->code;
   in_params = h->shared && h->nw <= cbk::kMaxParamWeights && c->dev.z >= 128;
@@ -683,6 +684,8 @@ cb_status nms_eval(cb_nms* h, const float* llr, int64_t n, const uint32_t* ref, 
   a.l_alpha = h->d_w;
   a.l_beta = h->d_w + h->nw;
   a.l_shared = h->shared;
+  // shared weights not in the launch parameters: each iteration's staged in shared memory
+  a.l_smem = h->shared && !param_w;
   CB_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), s));
   const int grid = (int)std::min<int64_t>(c->decode_grid, n);
   if (param_w) {

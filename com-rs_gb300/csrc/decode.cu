@@ -50,9 +50,13 @@ __host__ __device__ __forceinline__ size_t decode_smem_bytes(int n_full, int z, 
   return (b + 15) & ~(size_t)15;
 }
 
-// LEARNED (f32 only): the learned min-sum with per-edge, per-iteration weights la, lb
-template <typename T, bool LEARNED>
+// Weights of the learned min-sum (f32 only): none (the plain decoder), in global memory,
+// in the launch parameters, or each iteration's staged in shared memory
+enum LearnedWeights { kPlain = 0, kWeightsGlobal = 1, kWeightsParam = 2, kWeightsShared = 3 };
+
+template <typename T, int LW>
 __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float* la, const float* lb) {
+  constexpr bool LEARNED = LW != kPlain;
   extern __shared__ __align__(16) unsigned char smem[];
   const cbd::DevCode& c = a.code;
   const int z = c.z, nt = blockDim.x, tid = threadIdx.x;
@@ -109,6 +113,35 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
     if (some_check_fails(post, hd, s_ent, s_lstart, c.rows_n, ncol, z, tid, nt)) {
       it = max_it;
       for (int iter = 1; iter <= max_it; iter++) {
+        // learned weights of iterations iter - 2 (old messages) and iter - 1
+        const float *w_ap = nullptr, *w_bp = nullptr, *w_ac = nullptr, *w_bc = nullptr;
+        int w_stride = 1, w_roff = 0;
+        if constexpr (LEARNED) {
+          const int t = iter - 1, ne = c.n_entries;
+          if constexpr (LW == kWeightsShared) {
+            float* sw = reinterpret_cast<float*>(smem + decode_smem_bytes<T>(c.n_full, z, c.rows_n, c.n_entries));
+            float* cur = sw + (t & 1) * 2 * ne;
+            for (int i = tid; i < ne; i += nt) {
+              cur[i] = la[(size_t)t * ne + i];
+              cur[ne + i] = lb[(size_t)t * ne + i];
+            }
+            __syncthreads();
+            w_ac = cur;
+            w_bc = cur + ne;
+            w_ap = sw + ((t + 1) & 1) * 2 * ne;
+            w_bp = w_ap + ne;
+          } else {
+            const size_t per = a.l_shared ? (size_t)ne : (size_t)ne * z;
+            w_ac = la + (size_t)t * per;
+            w_bc = lb + (size_t)t * per;
+            w_ap = t > 0 ? w_ac - per : w_ac;
+            w_bp = t > 0 ? w_bc - per : w_bc;
+            if (!a.l_shared) {
+              w_stride = z;
+              w_roff = tid;
+            }
+          }
+        }
         // the state of a layer is prefetched one layer ahead
         T a1 = (T)0, a2 = (T)0;
         uint32_t mt = 0;
@@ -125,7 +158,7 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
             uint32_t nm;
             if constexpr (LEARNED)
               row_dispatch_learned(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z},
-                                   LearnedRowW{la, lb, c.n_entries, z, a.l_shared, s0, tid}, iter - 1,
+                                   LearnedRowW{w_ap, w_bp, w_ac, w_bc, s0, w_stride, w_roff}, iter - 1,
                                    iter == 1, a1, a2, mt, n1, n2, nm);
             else if constexpr (sizeof(T) == 4)
               row_dispatch_lean(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z}, a1, a2, mt, rule, alpha,
@@ -180,20 +213,21 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
   }
 }
 
-template <typename T, bool LEARNED>
+template <typename T, int LW>
 __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(const __grid_constant__ DecodeArgs<T> a) {
-  decode_body<T, LEARNED>(a, a.l_alpha, a.l_beta);
+  decode_body<T, LW>(a, a.l_alpha, a.l_beta);
 }
 
 __global__ void __launch_bounds__(384, 2) layered_learned_param_kernel(const __grid_constant__ LearnedParamArgs a) {
-  decode_body<float, true>(a.d, a.alpha, a.beta);
+  decode_body<float, kWeightsParam>(a.d, a.alpha, a.beta);
 }
 
 template <typename T>
-void* kernel_for(bool learned) {
-  if constexpr (sizeof(T) == 4)
-    if (learned) return (void*)layered_kernel<T, true>;
-  return (void*)layered_kernel<T, false>;
+void* kernel_for(const DecodeArgs<T>& a) {
+  if constexpr (sizeof(T) == 4) {
+    if (a.l_alpha) return a.l_smem ? (void*)layered_kernel<T, kWeightsShared> : (void*)layered_kernel<T, kWeightsGlobal>;
+  }
+  return (void*)layered_kernel<T, kPlain>;
 }
 
 int block_threads(int z) { return ((z + 31) / 32) * 32; }
@@ -211,7 +245,7 @@ size_t decode_state_bytes_per_slot(const cbd::DevCode& c, int precision) {
 }
 
 int decode_grid_size(const cbd::DevCode& c, int precision, int device) {
-  void* k = precision == 0 ? kernel_for<double>(false) : kernel_for<float>(false);
+  void* k = precision == 0 ? (void*)layered_kernel<double, kPlain> : (void*)layered_kernel<float, kPlain>;
   size_t smem = smem_bytes(c, precision);
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 0, sms = 0;
@@ -223,8 +257,8 @@ int decode_grid_size(const cbd::DevCode& c, int precision, int device) {
 template <typename T>
 cudaError_t launch_decode(const DecodeArgs<T>& a, int grid, cudaStream_t stream) {
   const int precision = sizeof(T) == 8 ? 0 : 1;
-  void* k = kernel_for<T>(a.l_alpha != nullptr);
-  size_t smem = smem_bytes(a.code, precision);
+  void* k = kernel_for<T>(a);
+  size_t smem = smem_bytes(a.code, precision) + (a.l_smem ? (size_t)4 * 4 * a.code.n_entries : 0);
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void* args[] = {(void*)&a};

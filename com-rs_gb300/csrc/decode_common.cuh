@@ -275,16 +275,15 @@ __device__ __forceinline__ void row_update_lean(float* __restrict__ post, const 
   nm = (sm << 8) | (uint32_t)i1;
 }
 
-// The learned min-sum's weights of one row: alpha and beta of (iteration t, entry s0 + e)
-// for lifted row r, shared by the Z rows or one per lifted edge (in global memory or in
-// the launch parameters).
+// The learned min-sum's weights of one row: alpha and beta of the previous and the
+// current iteration, entry s0 + e, lifted row r; `stride` 1 and `roff` 0 when shared by
+// the Z rows, else Z and r (global memory, launch parameters or shared memory).
 struct LearnedRowW {
-  const float* alpha;
-  const float* beta;
-  int n_entries, z, shared, s0, r;
-  __device__ __forceinline__ float magnitude(int t, int e, float m) const {
-    const size_t i = shared ? (size_t)t * n_entries + s0 + e : ((size_t)t * n_entries + s0 + e) * z + r;
-    const float am = __fsub_rn(__fmul_rn(alpha[i], m), beta[i]);
+  const float *a_prev, *b_prev, *a_cur, *b_cur;
+  int s0, stride, roff;
+  __device__ __forceinline__ float mag(const float* al, const float* be, int e, float m) const {
+    const int i = (s0 + e) * stride + roff;
+    const float am = __fsub_rn(__fmul_rn(al[i], m), be[i]);
     return am > 0.f ? am : 0.f;
   }
 };
@@ -308,7 +307,7 @@ __device__ __forceinline__ void row_update_learned(float* __restrict__ post, con
     if (first) {
       x[e] = __fsub_rn(p, 0.f);
     } else {
-      const float mag = w.magnitude(t - 1, e, (e == old_i1) ? a2 : a1);
+      const float mag = w.mag(w.a_prev, w.b_prev, e, (e == old_i1) ? a2 : a1);
       x[e] = ((t0 << e) & 0x80000000u) ? __fadd_rn(p, mag) : __fsub_rn(p, mag);
     }
   }
@@ -332,7 +331,7 @@ __device__ __forceinline__ void row_update_learned(float* __restrict__ post, con
   for (int e = 0; e < D; e++) {
     const bool eq = fabsf(x[e]) == m1;
     i1 = eq ? e : i1;
-    const float mag = w.magnitude(t, e, eq ? m2 : m1);
+    const float mag = w.mag(w.a_cur, w.b_cur, e, eq ? m2 : m1);
     const uint32_t ob = __float_as_uint(mag) | ((ps ^ __float_as_uint(x[e])) & 0x80000000u);
     st_post(post, off[e], __fadd_rn(x[e], __uint_as_float(ob)));
     sm = (sm << 1) | (ob >> 31);

@@ -29,6 +29,7 @@ struct DecodeArgs {
   const float* l_alpha = nullptr;
   const float* l_beta = nullptr;
   int32_t l_shared = 0;
+  int32_t l_smem = 0;  // 1: each iteration's (shared) weights staged in shared memory
 };
 
 // The learned decoder with its weights in the launch parameters (weights shared across

@@ -78,17 +78,19 @@ def test_training_gains_over_the_plain_min_sum(cb):
 
 
 @pytest.mark.parametrize("shared", [False, True])
-def test_fast_evaluation_equals_the_training_forward(cb, O, shared):
-    # the layered decoder with the network's weights (cb_nms_decode, cb_nms_run_frames)
-    # against the training forward (all T iterations, no stop): equal posteriors on every
-    # frame that runs all T iterations; the others stop on a codeword
+@pytest.mark.parametrize("k, e, z", [(520, 1040, 52), (1280, 2560, 128)])
+def test_fast_evaluation_equals_the_training_forward(cb, O, shared, k, e, z):
+    # the layered decoder with the network's weights (cb_nms_decode, cb_nms_run_frames;
+    # shared weights of Z >= 128 go in the launch parameters) against the training
+    # forward (all T iterations, no stop): equal posteriors on every frame that runs all
+    # T iterations; the others stop on a codeword
     T = 8
-    g = cb.NrLdpc(520, 1040, base_graph=2, lifting_size=52, precision="f32", max_iterations=T)
+    g = cb.NrLdpc(k, e, base_graph=2, lifting_size=z, precision="f32", max_iterations=T)
     net = cb.LearnedNms(g, T, shared=shared)
     rng = np.random.default_rng(7)
     net.set_weights((0.8 + 0.1 * rng.standard_normal(net.n_weights)).astype(np.float32),
                     (0.1 * rng.standard_normal(net.n_weights)).astype(np.float32))
-    ref = O.Code(520, 1040, bg=2, z=52)
+    ref = O.Code(k, e, bg=2, z=z)
     llr = np.concatenate([oracle_frames(O, ref, 32, eb)[0] for eb in (1.0, 3.0)])
     post, its = net.decode(llr)
     full = net.forward(llr)
@@ -102,5 +104,5 @@ def test_fast_evaluation_equals_the_training_forward(cb, O, shared):
     llr2, info2 = g.generate_frames(5, NAME, 0, 0, 64, 1.0, 4)
     post2, its2 = net.decode(llr2)
     assert np.array_equal(rec["iterations"], its2)
-    errs = ((post2[:, :520] < 0) != info2.astype(bool)).sum(axis=1)
+    errs = ((post2[:, :k] < 0) != info2.astype(bool)).sum(axis=1)
     assert np.array_equal(rec["bit_errors"], errs)
