@@ -23,6 +23,7 @@ import os
 import numpy as np
 
 from .campaign import Grid, Stop, run  # noqa: F401
+from .dvbs2 import Dvbs2Ldpc  # noqa: F401
 from .ldpc import Ldpc, parse_alist  # noqa: F401
 from .mix import MIX_ITEM_DTYPE, MixBatch, autotune, draw_mixed_batch  # noqa: F401
 

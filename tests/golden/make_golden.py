@@ -14,7 +14,8 @@ Outputs (committed):
     (flooding offset min-sum 0.15), ``..._flooding_spa_i50.json`` (flooding
     sum-product, 50 iterations) and ``ldpc_peg_n648_k540_layered_spa_i20.json``
     (layered sum-product), with their matrices ``peg_n576_k288.alist`` and
-    ``peg_n648_k540.alist``.
+    ``peg_n648_k540.alist``, and ``ldpc_dvbs2_short_r1_2_layered_spa_i50.json`` (the
+    DVB-S2 short rate-1/2 LDPC code, layered sum-product, 50 iterations).
 """
 
 import json
@@ -42,7 +43,8 @@ def main():
                "keys": sorted(k for k in out if not k.endswith(".shape"))},
               open(os.path.join(here, "sionna_nr_ldpc.json"), "w"), indent=1)
     for name in ("ldpc_peg_n576_k288_layered_nms075_i20", "ldpc_peg_n576_k288_flooding_oms015_i20",
-                 "ldpc_peg_n576_k288_flooding_spa_i50", "ldpc_peg_n648_k540_layered_spa_i20"):
+                 "ldpc_peg_n576_k288_flooding_spa_i50", "ldpc_peg_n648_k540_layered_spa_i20",
+                 "ldpc_dvbs2_short_r1_2_layered_spa_i50"):
         shutil.copy(os.path.join(root, "validation/aff3ct", name + ".json"), os.path.join(here, name + ".json"))
     for m in ("peg_n576_k288.alist", "peg_n648_k540.alist"):
         shutil.copy(os.path.join(root, "validation/aff3ct/matrices", m), os.path.join(here, m))
