@@ -167,17 +167,20 @@ def test_dvbs2_short_rate_half_overlaps_aff3ct(cb):
     # validation/tests/aff3ct.rs:231-233: the LDPC code of the short FECFRAME of rate 1/2,
     # layered sum-product, 50 iterations; BPSK over AWGN at sigma^2 = 1 / (2 R Eb/N0), R =
     # 4/9.  All-zero codewords (the decoders are symmetric, so the frame error rate does
-    # not depend on the codeword), frames capped at 12 288 per point.
+    # not depend on the codeword).  By default the points with FER >= 0.1 on 1024 frames
+    # each; COMRS_GB300_FULL=1 runs every point to 200 frame errors or 12 288 frames.
+    full = os.environ.get("COMRS_GB300_FULL") == "1"
     fx = json.load(open(os.path.join(GOLDEN, "ldpc_dvbs2_short_r1_2_layered_spa_i50.json")))
     code = cb.Dvbs2Ldpc("short", "1/2", max_iterations=50)
     num, den = fx["bit_rate"]
     rate = num / den
     rng = np.random.default_rng(11)
     checked = 0
-    for p in fx["data"]:
+    points = fx["data"] if full else [p for p in fx["data"] if p["fer"] >= 0.1]
+    for p in points:
         noise_var = 1.0 / (2.0 * rate * 10 ** (p["ebn0_db"] / 10))
         fe = nf = 0
-        while fe < 200 and nf < 12_288:
+        while fe < 200 and nf < (12_288 if full else 1024):
             y = 1.0 + np.sqrt(noise_var) * rng.standard_normal((1024, 16200))
             post, _ = code.decode_llr(2.0 * y / noise_var)
             fe += int((post < 0).any(axis=1).sum())
@@ -186,4 +189,4 @@ def test_dvbs2_short_rate_half_overlaps_aff3ct(cb):
         c_lo, c_hi = _wilson(fe, nf)
         assert not (a_hi < c_lo or c_hi < a_lo), (p["ebn0_db"], fe / nf, p["fer"])
         checked += 1
-    assert checked == len(fx["data"]) == 5
+    assert checked == (5 if full else 3)
