@@ -35,6 +35,7 @@ struct cb_ldpc {
   int grid = 0, threads = 0;
   size_t smem = 0;
   bool msgs_in_smem = false;
+  bool warp_rows = false;
   void* kernel = nullptr;
   cudaStream_t stream = nullptr;
   void* d_llr = nullptr;
@@ -101,9 +102,16 @@ cb_status ensure_device(cb_ldpc* c) {
   LDPC_CUDA(c, put(h.level_start, d.level_start));
   LDPC_CUDA(c, put(h.level_rows, d.level_rows));
   LDPC_CUDA(c, cudaMalloc(&c->d_counter, sizeof(unsigned long long)));
-  // threads: a level's rows (layered) or a share of the rows and variables (flooding)
-  const int want = c->layered ? h.max_level_rows : std::max(h.m, h.n) / 4;
-  c->threads = std::min(512, std::max(64, (want + 31) / 32 * 32));
+  // threads: a level's rows (layered), one warp per row when the levels hold few rows
+  // (at most 8) of at most 128 edges, else a thread per row; a share of the rows and
+  // variables (flooding)
+  c->warp_rows = c->layered && h.max_level_rows <= 8 && h.max_row_degree <= 128;
+  if (c->warp_rows) {
+    c->threads = 32 * h.max_level_rows;
+  } else {
+    const int want = c->layered ? h.max_level_rows : std::max(h.m, h.n) / 4;
+    c->threads = std::min(512, std::max(64, (want + 31) / 32 * 32));
+  }
   const size_t post_bytes = (size_t)h.n * elem(c);
   const size_t msg_bytes = (size_t)2 * h.edges * elem(c);
   c->msgs_in_smem = post_bytes + msg_bytes <= kSmemMsgBudget;
@@ -128,6 +136,7 @@ cb_status decode_impl(cb_ldpc* c, const T* llr, int64_t n, T* post, int32_t* ite
   a.alpha = c->alpha;
   a.max_iterations = c->max_iterations;
   a.msgs_in_smem = c->msgs_in_smem ? 1 : 0;
+  a.warp_rows = c->warp_rows ? 1 : 0;
   a.llr = llr;
   a.n_frames = n;
   a.post_out = post;

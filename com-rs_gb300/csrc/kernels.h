@@ -188,6 +188,7 @@ struct SparseArgs {
   double alpha;  // NMS scale or OMS offset
   int32_t max_iterations;
   int32_t msgs_in_smem;  // 1: the edge messages live in shared memory, else in `slots`
+  int32_t warp_rows;     // layered: one warp per row (levels of few rows), else one thread
   const T* llr;          // [n_frames][n]
   int64_t n_frames;
   T* post_out;           // [n_frames][n] (nullable)

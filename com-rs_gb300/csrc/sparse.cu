@@ -111,6 +111,111 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, T* post, 
   }
 }
 
+// One check node by a warp (layered schedule, levels of few rows): lane i takes edges
+// i, i + 32, ... of the row.  Min-sum: a warp reduction of (minimum, first index of the
+// minimum, second minimum) and of the sign parity gives the sequential loop's values
+// exactly (ties keep the first index, as the strict `<` does).  Sum-product: the
+// products of the other tanh(l/2) by warp scans, in chunks of 32 edges; the order of the
+// multiplications differs from the sequential one (a rounding difference, within the
+// tolerance the sum-product rule already has against the platform libm).
+template <typename T, int RULE>
+__device__ __forceinline__ void check_row_warp(const SparseDev& c, int row, T* post, T* msg, T alpha, int lane) {
+  const int e0 = c.row_start[row], e1 = c.row_start[row + 1];
+  if (RULE == cbd::RULE_SUM_PRODUCT) {
+    // first pass over the chunks (at most 4: rows of at most 128 edges): the incoming
+    // message, its tanh(l/2) and its exclusive prefix product, kept in registers; second
+    // pass from the last chunk: the suffix products and the outputs
+    T carry = (T)1;
+    T pre_r[4], t_r[4], l_r[4];
+    int nchunk = (e1 - e0 + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      pre_r[k] = (T)1;
+      t_r[k] = (T)1;
+      l_r[k] = (T)0;
+    }
+    for (int k = 0; k < nchunk && k < 4; k++) {
+      const int e = e0 + k * 32 + lane;
+      T l = (T)0, t = (T)1;
+      if (e < e1) {
+        l = sub_rn(post[c.vars[e]], msg[e]);
+        t = tanh_t(mul_rn(l, (T)0.5));
+      }
+      // inclusive scan of products within the chunk
+      T inc = t;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const T u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc = mul_rn(u, inc);
+      }
+      T exc = __shfl_up_sync(0xffffffffu, inc, 1);
+      if (lane == 0) exc = (T)1;
+      pre_r[k] = mul_rn(carry, exc);
+      t_r[k] = t;
+      l_r[k] = l;
+      carry = mul_rn(carry, __shfl_sync(0xffffffffu, inc, 31));
+    }
+    T scarry = (T)1;
+    for (int k = min(nchunk, 4) - 1; k >= 0; k--) {
+      const int e = e0 + k * 32 + lane;
+      T inc = t_r[k];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const T u = __shfl_down_sync(0xffffffffu, inc, o);
+        if (lane + o < 32) inc = mul_rn(u, inc);
+      }
+      T exc = __shfl_down_sync(0xffffffffu, inc, 1);
+      if (lane == 31) exc = (T)1;
+      const T suf = mul_rn(scarry, exc);
+      scarry = mul_rn(scarry, __shfl_sync(0xffffffffu, inc, 0));
+      if (e < e1) {
+        const T p = mul_rn(pre_r[k], suf);
+        const T o = mul_rn((T)2, atanh_t(clamp_t(p, -tanh_bound<T>(), tanh_bound<T>())));
+        msg[e] = o;
+        post[c.vars[e]] = add_rn(l_r[k], o);
+      }
+    }
+  } else {
+    int neg = 0, i1 = 0x7fffffff;
+    T m1 = infinity<T>(), m2 = infinity<T>();
+    for (int e = e0 + lane; e < e1; e += 32) {
+      const T l = sub_rn(post[c.vars[e]], msg[e]);
+      neg ^= (int)(l < (T)0);
+      const T a = fabs(l);
+      if (a < m1) {
+        m2 = m1;
+        m1 = a;
+        i1 = e - e0;
+      } else if (a < m2) {
+        m2 = a;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const T bm1 = __shfl_xor_sync(0xffffffffu, m1, o);
+      const T bm2 = __shfl_xor_sync(0xffffffffu, m2, o);
+      const int bi1 = __shfl_xor_sync(0xffffffffu, i1, o);
+      neg ^= __shfl_xor_sync(0xffffffffu, neg, o);
+      const bool mine = m1 < bm1 || (m1 == bm1 && i1 < bi1);
+      const T w2 = mine ? m2 : bm2, l1 = mine ? bm1 : m1;
+      m1 = mine ? m1 : bm1;
+      i1 = mine ? i1 : bi1;
+      m2 = fmin(w2, l1);
+    }
+    const T sign = neg ? (T)-1 : (T)1;
+    for (int e = e0 + lane; e < e1; e += 32) {
+      const int v = c.vars[e];
+      const T l = sub_rn(post[v], msg[e]);
+      const T s = mul_rn(sign, l < (T)0 ? (T)-1 : (T)1);
+      T mag = (e - e0) == i1 ? m2 : m1;
+      mag = RULE == cbd::RULE_NMS ? mul_rn(alpha, mag) : fmax(sub_rn(mag, alpha), (T)0);
+      const T o = mul_rn(s, mag);
+      msg[e] = o;
+      post[v] = add_rn(l, o);
+    }
+  }
+}
+
 // hard_decisions_are_a_codeword (ldpc.rs:555-557), CTA-wide
 template <typename T>
 __device__ __forceinline__ bool some_row_fails(const SparseDev& c, const T* post) {
@@ -158,7 +263,14 @@ __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ Spa
       T* cur = msg;   // flooding: the messages of the previous iteration
       T* next = aux;  // flooding: the new ones
       for (int iter = 1; iter <= a.max_iterations; iter++) {
-        if (LAYERED) {
+        if (LAYERED && a.warp_rows) {
+          const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+          for (int L = 0; L < c.levels; L++) {
+            const int r0 = c.level_start[L], r1 = c.level_start[L + 1];
+            for (int i = r0 + warp; i < r1; i += nw) check_row_warp<T, RULE>(c, c.level_rows[i], post, msg, alpha, lane);
+            __syncthreads();
+          }
+        } else if (LAYERED) {
           for (int L = 0; L < c.levels; L++) {
             const int r0 = c.level_start[L], r1 = c.level_start[L + 1];
             for (int i = r0 + tid; i < r1; i += nt) check_row<T, RULE, true>(c, c.level_rows[i], post, msg, nullptr, aux, alpha);
