@@ -335,6 +335,9 @@ class LearnedNms:
         return post, its
 
     def gradients(self, llr, cw, multi_loss=False):
+        """(mean loss, d/d scales, d/d offsets) of frames of E LLRs against their n_full
+        codeword bits.  multi_loss: 0 (False) the last output's loss, 1 (True) the mean over
+        every iteration's output, 2 their mean weighted 2 (t + 1) / (T (T + 1))."""
         x = np.ascontiguousarray(llr, np.float32).reshape(-1, self.code.e)
         c = np.ascontiguousarray(cw, np.uint8).reshape(-1, self.code.n_full)
         ga, gb = np.zeros(self.n_weights, np.float32), np.zeros(self.n_weights, np.float32)

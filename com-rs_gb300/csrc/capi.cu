@@ -726,7 +726,7 @@ cb_status nms_fwd_bwd(cb_nms* h, int64_t n, bool backward, int multi, cudaStream
   a.X = backward ? h->d_X : nullptr;
   a.loss = h->d_loss;
   a.P = h->d_P;
-  a.multi_loss = multi ? 1 : 0;
+  a.multi_loss = multi;
   CB_CUDA(c, cudaMemsetAsync(h->d_loss, 0, sizeof(float), s));
   CB_CUDA(c, cbk::launch_learned(a, true, s));
   if (backward) {
@@ -831,6 +831,7 @@ cb_status cb_nms_forward(cb_nms* h, const float* llr, int64_t n, float* post) {
 cb_status cb_nms_gradients(cb_nms* h, const float* llr, const uint8_t* cw, int64_t n, int32_t multi_loss,
                            float* g_alpha, float* g_beta, double* loss) {
   if (!h || !llr || !cw || n <= 0) return fail(nullptr, CB_ERR_CONFIG, "NULL argument or no frames");
+  if (multi_loss < 0 || multi_loss > 2) return fail(nullptr, CB_ERR_CONFIG, "multi_loss is 0, 1 or 2");
   cb_code* c = h->code;
   std::lock_guard<std::mutex> lock(c->mu);
   CB_CUDA(c, cudaSetDevice(c->device));
@@ -855,7 +856,8 @@ cb_status cb_nms_gradients(cb_nms* h, const float* llr, const uint8_t* cw, int64
 
 cb_status cb_nms_train_step(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_hash, int64_t batch, double lo,
                             double hi, double lr, int32_t multi_loss, double* loss) {
-  if (!h || batch <= 0 || !(hi >= lo) || !(lr > 0)) return fail(nullptr, CB_ERR_CONFIG, "bad training arguments");
+  if (!h || batch <= 0 || !(hi >= lo) || !(lr > 0) || multi_loss < 0 || multi_loss > 2)
+    return fail(nullptr, CB_ERR_CONFIG, "bad training arguments");
   cb_code* c = h->code;
   std::lock_guard<std::mutex> lock(c->mu);
   CB_CUDA(c, cudaSetDevice(c->device));

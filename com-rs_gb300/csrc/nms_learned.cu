@@ -12,8 +12,8 @@
 //
 // Training loss: the mean over frames and over the n_full codeword bits of
 // softplus(-(1 - 2 c_v) post_v), the binary cross-entropy of the soft output: of the
-// last iteration, or (multi-loss) averaged over the outputs of all T iterations, whose
-// posteriors the forward then saves.
+// last iteration, or (multi-loss) a weighted mean over the outputs of all T iterations,
+// whose posteriors the forward then saves: weights 1/T, or a ramp 2(t+1)/(T(T+1)).
 // Backward: for t = T-1..0 and the layers in reverse, each row recomputes its forward
 // quantities from the saved inputs x and propagates
 //   g_y = g_post[v] + g_c2v, g_a = g_y s [a > 0], dL/dalpha += g_a m, dL/dbeta -= g_a,
@@ -32,6 +32,12 @@ namespace {
 __device__ __forceinline__ size_t weight_index(const LearnedArgs& a, int t, int entry, int r) {
   return a.shared ? (size_t)t * a.code.n_entries + entry
                   : ((size_t)t * a.code.n_entries + entry) * a.code.z + r;
+}
+
+// weight of iteration t's output in the multi-loss: 1/T each (mode 1), or a linear ramp
+// 2 (t + 1) / (T (T + 1)) that leans on the last iterations (mode 2)
+__device__ __forceinline__ float iter_loss_weight(int mode, int t, int T) {
+  return mode == 2 ? 2.f * (float)(t + 1) / ((float)T * (float)(T + 1)) : 1.f / (float)T;
 }
 
 __device__ __forceinline__ float softplus_f(float x) { return x > 0.f ? x + log1pf(__expf(-x)) : log1pf(__expf(x)); }
@@ -253,7 +259,7 @@ __global__ void __launch_bounds__(384) learned_forward_kernel(const __grid_const
         for (int v = tid; v < c.n_full; v += nt) {
           Pt[v] = post[v];
           int bit = (a.cw_bits[(size_t)f * wpc + (v >> 5)] >> (v & 31)) & 1;
-          lsum += softplus_f(bit ? post[v] : -post[v]) / (float)a.T;
+          lsum += softplus_f(bit ? post[v] : -post[v]) * iter_loss_weight(a.multi_loss, t, a.T);
         }
       }
       if (stop && !some_check_fails(post, hd, s_ent, s_lstart, c.rows_n, ncol, z, tid, nt)) {
@@ -312,7 +318,7 @@ __global__ void __launch_bounds__(384) learned_backward_kernel(const __grid_cons
   const float* X = a.X + (size_t)f * a.T * edges;
   const int wpc = (c.n_full + 31) >> 5;
   const bool multi = a.multi_loss && a.P;
-  const float scale = 1.f / ((float)c.n_full * (float)a.n_frames * (multi ? (float)a.T : 1.f));
+  const float scale = 1.f / ((float)c.n_full * (float)a.n_frames);
   for (int v = tid; v < c.n_full; v += nt) gp[v] = 0.f;
   for (size_t i = tid; i < edges; i += nt) gc[i] = 0.f;
   if (tid < 38) red[tid] = 0.f;
@@ -322,10 +328,11 @@ __global__ void __launch_bounds__(384) learned_backward_kernel(const __grid_cons
     // the loss of iteration t's output (every iteration, or the last one)
     if (multi || t == a.T - 1) {
       const float* p = multi ? a.P + ((size_t)f * a.T + t) * c.n_full : a.post_out + (size_t)f * c.n_full;
+      const float sc = multi ? scale * iter_loss_weight(a.multi_loss, t, a.T) : scale;
       for (int v = tid; v < c.n_full; v += nt) {
         int bit = (a.cw_bits[(size_t)f * wpc + (v >> 5)] >> (v & 31)) & 1;
         float sgn = bit ? -1.f : 1.f;
-        gp[v] += -sgn * sigmoid_f(-sgn * p[v]) * scale;
+        gp[v] += -sgn * sigmoid_f(-sgn * p[v]) * sc;
       }
       __syncthreads();
     }

@@ -705,7 +705,7 @@ struct Learned {
   int T;
   bool shared;
   std::vector<int> lstart;  // base row -> first entry
-  bool multi = false;       // loss of every iteration's output (weight 1/T each), else the last
+  int multi = 0;  // 0: the last output's loss; 1: every iteration's, 1/T each; 2: ramp 2(t+1)/(T(T+1))
 };
 
 static void learned_layers(const Code& c, std::vector<int>& lstart) {
@@ -764,8 +764,9 @@ static double learned_frame(const Learned& L, const double* full_llr, const uint
     return l / (double)c.n;
   };
   double loss = 0.0;
+  auto weight = [&](int t) { return L.multi == 2 ? 2.0 * (t + 1) / ((double)T * (T + 1)) : 1.0 / (double)T; };
   if (L.multi)
-    for (int t = 0; t < T; t++) loss += bit_loss(&P[(size_t)t * c.n]) / (double)T;
+    for (int t = 0; t < T; t++) loss += bit_loss(&P[(size_t)t * c.n]) * weight(t);
   else
     loss = bit_loss(post.data());
   if (post_out) std::copy(post.begin(), post.end(), post_out);
@@ -780,7 +781,7 @@ static double learned_frame(const Learned& L, const double* full_llr, const uint
   };
   std::vector<double> gabs(32), gy(32);
   for (int t = T - 1; t >= 0; t--) {
-    if (L.multi) add_loss_grad(&P[(size_t)t * c.n], 1.0 / (double)T);
+    if (L.multi) add_loss_grad(&P[(size_t)t * c.n], weight(t));
     else if (t == T - 1) add_loss_grad(post.data(), 1.0);
     for (int Ly = rows_n - 1; Ly >= 0; Ly--)
       for (int r = 0; r < z; r++) {
@@ -1033,7 +1034,7 @@ void or_bpsk_llr_batch(void* h, uint64_t seed, uint64_t name_hash, uint64_t cond
 double or_learned(void* h, int T, int shared, int multi, const double* alpha, const double* beta, const double* llr,
                   const uint8_t* cw, int64_t n, double* post_out, double* ga, double* gb) {
   Code* c = (Code*)h;
-  Learned L{c, T, shared != 0, {}, multi != 0};
+  Learned L{c, T, shared != 0, {}, multi};
   learned_layers(*c, L.lstart);
   std::vector<double> full(c->n);
   double tot = 0.0;

@@ -39,7 +39,7 @@ def test_plain_weights_forward_is_the_min_sum(cb, O, shared):
     assert compared >= 10
 
 
-@pytest.mark.parametrize("shared,multi", [(False, False), (True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("shared,multi", [(False, 0), (True, 0), (False, 1), (True, 1), (False, 2), (True, 2)])
 def test_gradients_match_the_f64_oracle(cb, O, shared, multi):
     T = 5
     g = cb.NrLdpc(100, 300, base_graph=2, lifting_size=10, precision="f32")

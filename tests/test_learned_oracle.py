@@ -37,7 +37,7 @@ def test_plain_weights_are_the_min_sum(O, shared):
     assert compared >= 3
 
 
-@pytest.mark.parametrize("shared,multi", [(False, False), (True, False), (False, True)])
+@pytest.mark.parametrize("shared,multi", [(False, 0), (True, 0), (False, 1), (True, 2)])
 def test_gradients_match_finite_differences(O, shared, multi):
     code = O.Code(40, 80, bg=2, z=4)  # a small lifted code
     T = 4
