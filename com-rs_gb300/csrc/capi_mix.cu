@@ -376,8 +376,8 @@ cb_status cb_mix_classes(const cb_mix* m, int32_t capacity, int64_t* info, int32
 }
 
 cb_status cb_mix_set_rows_per_thread(cb_mix* m, int32_t cls, int32_t rho) {
-  if (!m || cls < 0 || cls >= (int32_t)m->classes.size() || (rho != 1 && rho != 2 && rho != 4))
-    return mfail(m, CB_ERR_CONFIG, "class index or rows per thread (1, 2 or 4)");
+  if (!m || cls < 0 || cls >= (int32_t)m->classes.size() || (rho != 1 && rho != 2))
+    return mfail(m, CB_ERR_CONFIG, "class index or rows per thread (1 or 2)");
   std::lock_guard<std::mutex> lock(m->mu);
   MIX_CUDA(m, cudaSetDevice(m->device));
   cbk::MixClass k = m->classes[cls];

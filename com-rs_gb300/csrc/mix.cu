@@ -79,10 +79,20 @@ __device__ void decode_item(const MixDecodeArgs& a, const MixItem& it, unsigned 
   float* post = reinterpret_cast<float*>(sm);
   uint32_t* hd = reinterpret_cast<uint32_t*>(post + 68 * z);
   uint32_t* s_ent = hd + ncol_max * ws;
-  uint16_t* s_lstart = reinterpret_cast<uint16_t*>(s_ent + cbh::kMaxEntries);
+  uint2* s_addr = reinterpret_cast<uint2*>(s_ent + cbh::kMaxEntries);
+  uint16_t* s_lstart = reinterpret_cast<uint16_t*>(s_addr + cbh::kMaxEntries);
+  uint8_t* s_order = reinterpret_cast<uint8_t*>(s_lstart + cbh::kMaxLayers + 1);
+  uint8_t* s_end = s_order + cbh::kMaxLayers;
   const int ncol = c.n_full / z;
-  for (int i = lt; i < c.n_entries; i += nt) s_ent[i] = c.entry[i];
+  for (int i = lt; i < c.n_entries; i += nt) {
+    s_ent[i] = c.entry[i];
+    s_addr[i] = c.eaddr[i];
+  }
   for (int i = lt; i <= c.rows_n; i += nt) s_lstart[i] = c.layer_start[i];
+  for (int i = lt; i < c.rows_n; i += nt) {
+    s_order[i] = c.layer_order[i];
+    s_end[i] = c.level_end[i];
+  }
   const float* llr = a.llr + it.llr_offset;
   for (int v = lt; v < c.n_full; v += nt) post[v] = 0.f;
   slot_sync(bar, nt);
@@ -103,9 +113,11 @@ __device__ void decode_item(const MixDecodeArgs& a, const MixItem& it, unsigned 
         a1[q] = a2[q] = 0.f;
         mt[q] = 0u;
         const int r = lt + q * nt;
-        if (iter > 1 && r < z) st.load(r, a1[q], a2[q], mt[q]);
+        if (iter > 1 && r < z) st.load(s_order[0] * z + r, a1[q], a2[q], mt[q]);
       }
-      for (int L = 0; L < rows_n; L++) {
+      // the base rows by levels, as decode.cu runs them
+      for (int k = 0; k < rows_n; k++) {
+        const int L = s_order[k];
         float p1[RHO], p2[RHO];
         uint32_t pm[RHO];
 #pragma unroll
@@ -113,7 +125,7 @@ __device__ void decode_item(const MixDecodeArgs& a, const MixItem& it, unsigned 
           p1[q] = p2[q] = 0.f;
           pm[q] = 0u;
           const int r = lt + q * nt;
-          if (iter > 1 && r < z && L + 1 < rows_n) st.load((L + 1) * z + r, p1[q], p2[q], pm[q]);
+          if (iter > 1 && r < z && k + 1 < rows_n) st.load(s_order[k + 1] * z + r, p1[q], p2[q], pm[q]);
         }
         const int s0 = s_lstart[L], d = s_lstart[L + 1] - s0;
 #pragma unroll
@@ -122,14 +134,15 @@ __device__ void decode_item(const MixDecodeArgs& a, const MixItem& it, unsigned 
           if (r < z) {
             float n1, n2;
             uint32_t nm;
-            row_dispatch<float>(d, post, s_ent + s0, r, z, a1[q], a2[q], mt[q], a.rule, a.alpha, n1, n2, nm);
+            row_dispatch_lean(d, post, EdgeAddrTable{s_addr + s0, r, 4 * r, 4 * z}, a1[q], a2[q], mt[q], a.rule,
+                              a.alpha, n1, n2, nm);
             st.store(L * z + r, n1, n2, nm);
           }
           a1[q] = p1[q];
           a2[q] = p2[q];
           mt[q] = pm[q];
         }
-        slot_sync(bar, nt);
+        if (s_end[k]) slot_sync(bar, nt);
       }
       if (!slot_check_fails(post, hd, s_ent, s_lstart, rows_n, ncol, z, lt, nt, bar, flag)) {
         iters = iter;
@@ -185,8 +198,7 @@ __global__ void __launch_bounds__(384, 2) mix_decode_kernel(const __grid_constan
         if (i >= cls.count) break;
         const MixItem it = a.items[cls.first + i];
         if (cls.rows_per_thread == 1) decode_item<1>(a, it, sm, cls.max_ncol, st, lt, nt, bar, &s_flag[slot], &s_err[slot]);
-        else if (cls.rows_per_thread == 2) decode_item<2>(a, it, sm, cls.max_ncol, st, lt, nt, bar, &s_flag[slot], &s_err[slot]);
-        else decode_item<4>(a, it, sm, cls.max_ncol, st, lt, nt, bar, &s_flag[slot], &s_err[slot]);
+        else decode_item<2>(a, it, sm, cls.max_ncol, st, lt, nt, bar, &s_flag[slot], &s_err[slot]);
       }
     }
     __syncthreads();
@@ -197,7 +209,8 @@ __global__ void __launch_bounds__(384, 2) mix_decode_kernel(const __grid_constan
 
 size_t mix_slot_smem_bytes(int z) {
   const int ws = (z + 31) / 32 + 1;
-  size_t b = (size_t)68 * z * 4 + (size_t)68 * ws * 4 + (size_t)cbh::kMaxEntries * 4 + (size_t)(cbh::kMaxLayers + 1) * 2;
+  size_t b = (size_t)68 * z * 4 + (size_t)68 * ws * 4 + (size_t)cbh::kMaxEntries * (4 + 8) +
+             (size_t)(cbh::kMaxLayers + 1) * 2 + (size_t)cbh::kMaxLayers * 2;
   return (b + 15) & ~(size_t)15;
 }
 

@@ -6,7 +6,7 @@
   circular buffer (the rate rule of the uneven-mix benchmark);
 * :class:`MixBatch` -- the C ABI's cb_mix: generate and decode the batch by one
   replayed CUDA graph, records in the items' order;
-* :func:`autotune` -- per lifting-size class, the lifted rows per thread (1, 2 or 4)
+* :func:`autotune` -- per lifting-size class, the lifted rows per thread (1 or 2)
   whose timed decode phase is fastest, cached per device and lifting size.
 """
 
@@ -107,6 +107,10 @@ class MixBatch:
         return ms.value
 
 
+# the rows per thread the mixed decoder is compiled for
+ROWS_PER_THREAD = (1, 2)
+
+
 def _cache_path():
     base = os.environ.get("COMRS_GB300_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "comrs_gb300")
     return os.path.join(base, "mix_autotune.json")
@@ -133,11 +137,11 @@ def autotune(batch, reps=3, cache=True, device_name=None):
     chosen = {}
     for k, cls in enumerate(batch.classes()):
         key = str(cls["z"])
-        if cache and key in dev:
+        if cache and key in dev and dev[key].get("rows_per_thread") in ROWS_PER_THREAD:
             rho, times = dev[key]["rows_per_thread"], dev[key]["ms"]
         else:
             times = {}
-            for rho in (1, 2, 4):
+            for rho in ROWS_PER_THREAD:
                 try:
                     batch.set_rows_per_thread(k, rho)
                 except Exception:

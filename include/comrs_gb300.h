@@ -203,7 +203,7 @@ const char* cb_mix_last_error(const cb_mix* mix);
 /* per class (up to `capacity`), 8 values: Z, codewords, rows per thread, slots per
  * CTA, threads per slot, shared bytes per slot, resident CTAs, first sorted item */
 cb_status cb_mix_classes(const cb_mix* mix, int32_t capacity, int64_t* info, int32_t* n_classes);
-/* the autotuner's knob: lifted rows per thread (1, 2 or 4) of one class */
+/* the autotuner's knob: lifted rows per thread (1 or 2) of one class */
 cb_status cb_mix_set_rows_per_thread(cb_mix* mix, int32_t class_index, int32_t rows_per_thread);
 /* generate and decode the batch at `epoch` (replays the graph); records in the items'
  * order into `out` (host, n_items records; NULL to skip the copy) */

@@ -42,7 +42,7 @@ def test_rows_per_thread_do_not_change_the_records(cb):
     mix = cb.MixBatch(items, seed=7, name=NAME, max_iterations=25)
     base = mix.run(0)
     for k, c in enumerate(mix.classes()):
-        for rho in (2, 4):
+        for rho in (2,):
             try:
                 mix.set_rows_per_thread(k, rho)
             except cb.ComrsError:
