@@ -33,6 +33,7 @@
 #include <cuda_runtime.h>
 
 #include "crmath.cuh"
+#include "decode_common.cuh"
 #include "kernels.h"
 
 namespace cbk {
@@ -42,15 +43,88 @@ constexpr int NT = kGenThreads;
 
 __device__ __forceinline__ int gray(int i) { return i ^ (i >> 1); }
 
+// f32 noise and max-log (or exact) demapping of the symbols [s0, s1) of a frame, H bits
+// per dimension.  The square QAM's label is gray(row) * side + gray(col): the first H
+// bits come from the imaginary part, the last H from the real part, so each bit's LLR is
+// a one-dimensional max-log (exact: log-sum-exp) over the side levels of its dimension;
+// the level metrics of both dimensions are computed once per symbol.
+template <int H, typename T>
+__device__ __forceinline__ void noise_demap_f32(const cbd::DevCode& c, const GenFrame<T>& a, cbd::Xoshiro& r,
+                                                const uint8_t* lab, const double* pts, int s0, int s1, float sd,
+                                                float inv_s2, T* out) {
+  constexpr int SIDE = 1 << H, MB = 2 * H;
+  // the PAM levels of each dimension, ascending: real level q is point gray(q),
+  // imaginary level q is point gray(side - 1 - q) * side
+  float lev_re[SIDE], lev_im[SIDE];
+#pragma unroll
+  for (int q = 0; q < SIDE; q++) {
+    lev_re[q] = (float)pts[2 * gray(q)];
+    lev_im[q] = (float)pts[2 * (gray(SIDE - 1 - q) * SIDE) + 1];
+  }
+  for (int s = s0; s < s1; s++) {
+    uint64_t x1 = cbd::xoshiro_next(r) >> 11, x2 = cbd::xoshiro_next(r) >> 11;
+    // 1 - u1 = (2^53 - x1) 2^-53 exactly, then rounded once to f32
+    float one_minus_u1 = __ull2float_rn((1ull << 53) - x1) * 1.1102230246251565e-16f;
+    float u2 = __ull2float_rn(x2 >> 29) * 5.9604644775390625e-08f;  // top 24 bits of u2
+    float rad = sqrtf(-2.0f * logf(one_minus_u1)) * 0.70710678f;
+    float sn, cs;
+    sincospif(2.0f * u2, &sn, &cs);
+    int li = lab[s];
+    float yre = (float)pts[2 * li] + rad * cs * sd;
+    float yim = (float)pts[2 * li + 1] + rad * sn * sd;
+    float met_re[SIDE], met_im[SIDE];
+#pragma unroll
+    for (int q = 0; q < SIDE; q++) {
+      float dr = yre - lev_re[q], di = yim - lev_im[q];
+      met_re[q] = -(dr * dr) * inv_s2;
+      met_im[q] = -(di * di) * inv_s2;
+    }
+#pragma unroll
+    for (int o = 0; o < MB; o++) {
+      const int t = s * MB + o;
+      if (t >= c.e) break;
+      const bool upper = o < H;
+      const int bitpos = upper ? (H - 1 - o) : (MB - 1 - o);
+      float m0 = -INFINITY, m1 = -INFINITY;
+#pragma unroll
+      for (int q = 0; q < SIDE; q++) {
+        const int lbl = upper ? gray(SIDE - 1 - q) : gray(q);
+        const float met = upper ? met_im[q] : met_re[q];
+        if ((lbl >> bitpos) & 1) m1 = fmaxf(m1, met);
+        else m0 = fmaxf(m0, met);
+      }
+      if (a.exact) {
+        // exact log-sum-exp per dimension: the other dimension's sum is common to both
+        // halves of the labels and cancels
+        float e0 = 0.f, e1 = 0.f;
+#pragma unroll
+        for (int q = 0; q < SIDE; q++) {
+          const int lbl = upper ? gray(SIDE - 1 - q) : gray(q);
+          const float met = upper ? met_im[q] : met_re[q];
+          if ((lbl >> bitpos) & 1) e1 += expf(met - m1);
+          else e0 += expf(met - m0);
+        }
+        out[t] = (T)(m0 + logf(e0) - m1 - logf(e1));
+      } else {
+        out[t] = (T)(m0 - m1);
+      }
+    }
+  }
+}
+
 // One frame by one CTA of NT threads: code `c`, frame parameters `a`.
 template <typename T>
 __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>& a, unsigned char* smem) {
   const int z = c.z, tid = threadIdx.x;
   const int n_sym = (c.e + a.n_pad) / a.mbits;
-  // shared layout: points (2M doubles) | syndromes (4Z) | codeword (n_full) | labels
+  const int wz = (z + 31) >> 5, ws = wz + 1, ncol = c.n_full / z;
+  // shared layout: points (2M doubles) | packed codeword columns (ncol x ws words: Z bits
+  // each, then a zero word) | packed core syndromes (4 x ws) | codeword bytes (n_full) |
+  // labels
   double* pts = reinterpret_cast<double*>(smem);
-  uint8_t* syn = reinterpret_cast<uint8_t*>(pts + 2 * a.m);
-  uint8_t* cw = syn + 4 * z;
+  uint32_t* cwp = reinterpret_cast<uint32_t*>(pts + 2 * a.m);
+  uint32_t* synp = cwp + ncol * ws;
+  uint8_t* cw = reinterpret_cast<uint8_t*>(synp + 4 * ws);
   uint8_t* lab = cw + c.n_full;
   uint8_t* pad = lab + n_sym;  // padding bits (< mbits)
   __shared__ double s_sigma2;
@@ -83,49 +157,74 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
       if (lane == 0) a.info_out[b0 >> 5] = word;
     }
   }
-  // ---- encoder: core syndromes over the systematic columns
-  for (int task = tid; task < 4 * z; task += NT) {
-    int L = task / z, r = task - L * z;
+  // ---- encoder on packed columns, 32 lifted rows per word: the rows r0 .. r0 + 31 of an
+  // entry (j, s) read the Z-bit column j from bit (r0 + s) mod Z on (window32, wrapping
+  // at Z); the XOR over a row's entries is then the parity of 32 rows at once
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int task = warp; task < c.cols_k * wz; task += NT / 32) {  // pack the systematic columns
+    const int j = task / wz, w = task - j * wz, b = w * 32 + lane;
+    const uint32_t word = __ballot_sync(0xffffffffu, b < z && cw[j * z + b]);
+    if (lane == 0) {
+      cwp[j * ws + w] = word;
+      if (w == wz - 1) cwp[j * ws + wz] = 0u;
+    }
+  }
+  __syncthreads();
+  // the 32-row window of a packed Z-bit column from row r0 with shift s (rows past Z read 0)
+  auto window = [&](const uint32_t* col, int r0, int shift) -> uint32_t {
+    int o = r0 + shift;
+    o -= (o >= z) ? z : 0;
+    uint32_t win = window32(col, o);
+    const int nrows = min(32, z - r0);
+    if (o + nrows > z) win |= window32(col, 0) << (z - o);
+    return nrows == 32 ? win : (win & ((1u << nrows) - 1u));
+  };
+  // core syndromes over the systematic columns
+  for (int task = tid; task < 4 * wz; task += NT) {
+    const int L = task / wz, g = task - L * wz;
     uint32_t acc = 0;
     for (int t = c.layer_start[L]; t < c.layer_start[L + 1]; t++) {
-      uint32_t en = c.entry[t];
-      int j = (int)(en >> 16);
-      if (j >= c.cols_k) continue;
-      int cc = r + (int)(en & 0xffffu);
-      cc -= (cc >= z) ? z : 0;
-      acc ^= cw[j * z + cc];
+      const uint32_t en = c.entry[t];
+      const int j = (int)(en >> 16);
+      if (j < c.cols_k) acc ^= window(cwp + j * ws, g * 32, (int)(en & 0xffffu));
     }
-    syn[task] = (uint8_t)acc;
+    synp[L * ws + g] = acc;
+    if (g == wz - 1) synp[L * ws + wz] = 0u;
   }
   __syncthreads();
   // core parity: block-circulant inverse of the core
-  for (int task = tid; task < 4 * z; task += NT) {
-    int blk = task / z, r = task - blk * z;
+  for (int task = tid; task < 4 * wz; task += NT) {
+    const int blk = task / wz, g = task - blk * wz;
     uint32_t acc = 0;
     for (int t = 0; t < c.n_core_terms; t++) {
-      uint32_t ct = c.core_term[t];
+      const uint32_t ct = c.core_term[t];
       if ((int)(ct >> 20) != blk) continue;
-      int src = (int)((ct >> 16) & 15u);
-      int cc = r + (int)(ct & 0xffffu);
-      cc -= (cc >= z) ? z : 0;
-      acc ^= syn[src * z + cc];
+      acc ^= window(synp + (int)((ct >> 16) & 15u) * ws, g * 32, (int)(ct & 0xffffu));
     }
-    cw[c.k + task] = (uint8_t)acc;
+    uint32_t* col = cwp + (c.cols_k + blk) * ws;
+    col[g] = acc;
+    if (g == wz - 1) col[wz] = 0u;
   }
   __syncthreads();
-  // extension parity: row L >= 4 closes on its own parity bit k + L z + r
-  for (int task = 4 * z + tid; task < c.rows_n * z; task += NT) {
-    int L = task / z, r = task - L * z;
+  // extension parity: row L >= 4 closes on its own column cols_k + L (shift 0) and reads
+  // only systematic and core parity columns
+  for (int task = 4 * wz + tid; task < c.rows_n * wz; task += NT) {
+    const int L = task / wz, g = task - L * wz;
     uint32_t acc = 0;
-    int own = c.k + task;
     for (int t = c.layer_start[L]; t < c.layer_start[L + 1]; t++) {
-      int col = (int)(c.entry[t] >> 16) * z;
-      int cc = r + (int)(c.entry[t] & 0xffffu);
-      cc -= (cc >= z) ? z : 0;
-      col += cc;
-      if (col != own) acc ^= cw[col];
+      const uint32_t en = c.entry[t];
+      const int j = (int)(en >> 16);
+      if (j != c.cols_k + L) acc ^= window(cwp + j * ws, g * 32, (int)(en & 0xffffu));
     }
-    cw[own] = (uint8_t)acc;
+    uint32_t* col = cwp + (c.cols_k + L) * ws;
+    col[g] = acc;
+    if (g == wz - 1) col[wz] = 0u;
+  }
+  __syncthreads();
+  // the parity bits back to bytes, for the labels
+  for (int v = c.k + tid; v < c.n_full; v += NT) {
+    const int j = v / z, b = v - j * z;
+    cw[v] = (uint8_t)((cwp[j * ws + (b >> 5)] >> (b & 31)) & 1u);
   }
   __syncthreads();
   if (a.cw_out) {  // the full codeword, packed
@@ -228,61 +327,14 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
   } else {
     const float sd = (float)__dsqrt_rn(sigma2);
     const float inv_s2 = (float)(1.0 / sigma2);
-    const int h = a.mbits >> 1, side = 1 << h;
-    // the PAM levels of each dimension, ascending, with their Gray label parts:
-    // real level q is point gray(q), imaginary level q is point gray(side - 1 - q) * side
-    float lev_re[16], lev_im[16];
-    for (int q = 0; q < side; q++) {
-      lev_re[q] = (float)pts[2 * gray(q)];
-      lev_im[q] = (float)pts[2 * (gray(side - 1 - q) * side) + 1];
-    }
-    for (int s = s0; s < s1; s++) {
-      uint64_t x1 = cbd::xoshiro_next(r) >> 11, x2 = cbd::xoshiro_next(r) >> 11;
-      // 1 - u1 = (2^53 - x1) 2^-53 exactly, then rounded once to f32
-      float one_minus_u1 = __ull2float_rn((1ull << 53) - x1) * 1.1102230246251565e-16f;
-      float u2 = __ull2float_rn(x2 >> 29) * 5.9604644775390625e-08f;  // top 24 bits of u2
-      float rad = sqrtf(-2.0f * logf(one_minus_u1)) * 0.70710678f;
-      float sn, cs;
-      sincospif(2.0f * u2, &sn, &cs);
-      int li = lab[s];
-      float yre = (float)pts[2 * li] + rad * cs * sd;
-      float yim = (float)pts[2 * li + 1] + rad * sn * sd;
-      // label = gray(row) * side + gray(col): the first h bits come from the
-      // imaginary part, the last h from the real part
-      for (int o = 0; o < a.mbits; o++) {
-        int t = s * a.mbits + o;
-        if (t >= c.e) break;
-        bool upper = o < h;
-        int bitpos = upper ? (h - 1 - o) : (a.mbits - 1 - o);
-        float y = upper ? yim : yre;
-        float m0 = -INFINITY, m1 = -INFINITY;
-        for (int q = 0; q < side; q++) {
-          int lbl = upper ? gray(side - 1 - q) : gray(q);
-          float dd = y - (upper ? lev_im[q] : lev_re[q]);
-          float met = -(dd * dd) * inv_s2;
-          if ((lbl >> bitpos) & 1) m1 = fmaxf(m1, met);
-          else m0 = fmaxf(m0, met);
-        }
-        if (a.exact) {
-          // exact log-sum-exp per dimension: the other dimension's sum is common to
-          // both halves of the labels and cancels
-          float s0 = 0.f, s1 = 0.f;
-          for (int q = 0; q < side; q++) {
-            int lbl = upper ? gray(side - 1 - q) : gray(q);
-            float dd = y - (upper ? lev_im[q] : lev_re[q]);
-            float met = -(dd * dd) * inv_s2;
-            if ((lbl >> bitpos) & 1) s1 += expf(met - m1);
-            else s0 += expf(met - m0);
-          }
-          out[t] = (T)(m0 + logf(s0) - m1 - logf(s1));
-        } else {
-          out[t] = (T)(m0 - m1);
-        }
-      }
+    switch (a.mbits) {
+      case 2: noise_demap_f32<1>(c, a, r, lab, pts, s0, s1, sd, inv_s2, out); break;
+      case 4: noise_demap_f32<2>(c, a, r, lab, pts, s0, s1, sd, inv_s2, out); break;
+      case 6: noise_demap_f32<3>(c, a, r, lab, pts, s0, s1, sd, inv_s2, out); break;
+      default: noise_demap_f32<4>(c, a, r, lab, pts, s0, s1, sd, inv_s2, out); break;
     }
   }
 }
-
 
 template <typename T>
 __global__ void __launch_bounds__(NT) gen_kernel(const __grid_constant__ GenArgs<T> a) {
@@ -346,7 +398,8 @@ __global__ void __launch_bounds__(NT) gen_mix_kernel(const __grid_constant__ Gen
 
 size_t gen_smem_bytes(const cbd::DevCode& c, int m, int mbits, int n_pad) {
   int n_sym = (c.e + n_pad) / mbits;
-  return (size_t)2 * m * sizeof(double) + 4 * c.z + c.n_full + n_sym + 16;
+  const int ws = (c.z + 31) / 32 + 1, ncol = c.n_full / c.z;
+  return (size_t)2 * m * sizeof(double) + (size_t)(ncol + 4) * ws * 4 + c.n_full + n_sym + 16;
 }
 
 template <typename T>
