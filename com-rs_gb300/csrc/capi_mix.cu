@@ -78,7 +78,7 @@ void layout(cbk::MixClass& k, int rho) {
   int by_threads = kCtaThreads / k.slot_threads;
   int by_smem = (int)(kSlotSmemBudget / (size_t)k.smem_per_slot);
   k.slots = std::min({by_threads, by_smem, 15});
-  k.state_per_slot = (int32_t)((size_t)cbh::kMaxLayers * k.z * 16);
+  k.state_per_slot = (int32_t)((size_t)cbh::kMaxLayers * k.z * 12);
   k.max_ncol = 68;
 }
 

@@ -397,11 +397,12 @@ __device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent
   }
 }
 
-// check-node state of one lifted row: f32 as one 16-byte record {n1, n2, meta, 0};
-// f64 as a 16-byte {n1, n2} record plus a separate plane of meta words
+// check-node state of one lifted row: f32 as an 8-byte {n1, n2} record plus a plane of
+// meta words (12 bytes a row, so more of the slots stay in L2); f64 as a 16-byte
+// {n1, n2} record plus a plane of meta words
 template <typename T>
 struct StateSlot;
-// The state records of all resident CTAs (86 MB at BG1 Z = 384) fit in L2, but the LLR
+// The state records of all resident CTAs (64 MB at BG1 Z = 384) fit in L2, but the LLR
 // stream of a launch (830 MB for 8192 codewords) would evict them: the records are read
 // and written with an L2 evict-last policy, the LLRs with streaming loads.
 __device__ __forceinline__ uint64_t l2_evict_last_policy() {
@@ -410,30 +411,30 @@ __device__ __forceinline__ uint64_t l2_evict_last_policy() {
   return pol;
 }
 
+// f32 state in two planes: {n1, n2} (8 bytes) and the meta word (4 bytes)
 template <>
 struct StateSlot<float> {
-  uint4* rec;
+  uint2* mag;
+  uint32_t* meta;
   uint64_t pol;
   __device__ __forceinline__ StateSlot(unsigned char* base, int rows)
-      : rec(reinterpret_cast<uint4*>(base)), pol(l2_evict_last_policy()) {
-    (void)rows;
-  }
+      : mag(reinterpret_cast<uint2*>(base)), meta(reinterpret_cast<uint32_t*>(base + (size_t)rows * 8)),
+        pol(l2_evict_last_policy()) {}
   __device__ __forceinline__ void load(int row, float& a1, float& a2, uint32_t& mt) const {
-    uint32_t x, y, zz, w;
-    asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
-                 : "=r"(x), "=r"(y), "=r"(zz), "=r"(w)
-                 : "l"(rec + row), "l"(pol));
-    (void)w;
+    uint32_t x, y, w;
+    asm volatile("ld.global.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(x), "=r"(y) : "l"(mag + row), "l"(pol));
+    asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(w) : "l"(meta + row), "l"(pol));
     a1 = __uint_as_float(x);
     a2 = __uint_as_float(y);
-    mt = zz;
+    mt = w;
   }
   __device__ __forceinline__ void store(int row, float n1, float n2, uint32_t nm) const {
-    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(rec + row),
-                 "r"(__float_as_uint(n1)), "r"(__float_as_uint(n2)), "r"(nm), "r"(0u), "l"(pol)
+    asm volatile("st.global.L2::cache_hint.v2.u32 [%0], {%1, %2}, %3;" ::"l"(mag + row), "r"(__float_as_uint(n1)),
+                 "r"(__float_as_uint(n2)), "l"(pol)
                  : "memory");
+    asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(meta + row), "r"(nm), "l"(pol) : "memory");
   }
-  static __host__ __device__ size_t bytes(int rows) { return (size_t)rows * 16; }
+  static __host__ __device__ size_t bytes(int rows) { return (size_t)rows * 12; }
 };
 template <>
 struct StateSlot<double> {

@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(384, 2) mix_decode_kernel(const __grid_constan
       const int lt = tid - slot * cls.slot_threads, nt = cls.slot_threads, bar = slot + 1;
       unsigned char* sm = smem + (size_t)slot * cls.smem_per_slot;
       const StateSlot<float> st(a.state + (size_t)blockIdx.x * a.state_per_cta + (size_t)slot * cls.state_per_slot,
-                                0);
+                                cbh::kMaxLayers * cls.z);
       for (;;) {
         if (lt == 0) s_item[slot] = (long long)atomicAdd(&a.counters[k], 1ull);
         slot_sync(bar, nt);
