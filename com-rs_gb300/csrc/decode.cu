@@ -92,7 +92,21 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
     for (int v = tid; v < c.n_full; v += nt) post[v] = (T)0;
     __syncthreads();
     if (c.map_is_offset) {
-      for (int t = tid; t < c.e; t += nt) post[2 * z + t] = add_rn((T)0, __ldcs(llr + t));
+      if (sizeof(T) == 4 && (c.e & 3) == 0 && (reinterpret_cast<uintptr_t>(a.llr) & 15) == 0) {
+        // 128-bit streaming loads: a 16-byte aligned buffer with E % 4 == 0 keeps every
+        // frame's row 16-byte aligned (any other buffer takes the 32-bit loads below)
+        const float4* l4 = reinterpret_cast<const float4*>(llr);
+        for (int q = tid; q < (c.e >> 2); q += nt) {
+          const float4 v = __ldcs(l4 + q);
+          T* d = post + 2 * z + 4 * q;
+          d[0] = add_rn((T)0, (T)v.x);
+          d[1] = add_rn((T)0, (T)v.y);
+          d[2] = add_rn((T)0, (T)v.z);
+          d[3] = add_rn((T)0, (T)v.w);
+        }
+      } else {
+        for (int t = tid; t < c.e; t += nt) post[2 * z + t] = add_rn((T)0, __ldcs(llr + t));
+      }
     } else if (!c.has_repeats) {
       for (int t = tid; t < c.e; t += nt) post[c.map[t]] = add_rn((T)0, __ldcs(llr + t));
     } else {

@@ -147,3 +147,27 @@ def test_many_frames_in_one_launch(cb, O):
     bits, app, it = g.decode_full(big)
     bits1, app1, it1 = g.decode_full(llr)
     assert np.array_equal(bits, np.tile(bits1, (60, 1))) and np.array_equal(it, np.tile(it1, 60))
+
+
+def test_decode_device_accepts_a_buffer_of_any_alignment(cb):
+    # the f32 decoder loads the LLRs 128 bits at a time from 16-byte aligned buffers and
+    # 32 bits at a time from any other: both give the same results
+    import ctypes as C
+
+    import torch
+
+    g = cb.NrLdpc(8448, 25344, base_graph=1, lifting_size=384, precision="f32")
+    llr, _ = g.generate_frames(7, "align", 0, 0, 16, 1.5, 16)
+    flat = torch.zeros(16 * 25344 + 4, dtype=torch.float32, device="cuda")
+    outs = []
+    for off in (0, 1):
+        flat[off:off + 16 * 25344] = torch.from_numpy(llr.reshape(-1)).cuda()
+        bits = torch.zeros((16, 264), dtype=torch.int32, device="cuda")
+        its = torch.zeros(16, dtype=torch.int32, device="cuda")
+        st = cb.lib().cb_decode_device(g._h, C.c_void_p(flat.data_ptr() + 4 * off), 16, C.c_void_p(bits.data_ptr()),
+                                       None, C.c_void_p(its.data_ptr()), None)
+        assert st == 0
+        torch.cuda.synchronize()
+        outs.append((bits.cpu(), its.cpu()))
+    assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+    assert torch.equal(outs[0][0].numpy().view("u4").astype("u4")[:, :1], outs[0][0].numpy().view("u4")[:, :1])
