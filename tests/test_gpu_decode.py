@@ -164,10 +164,15 @@ def test_decode_device_accepts_a_buffer_of_any_alignment(cb):
         flat[off:off + 16 * 25344] = torch.from_numpy(llr.reshape(-1)).cuda()
         bits = torch.zeros((16, 264), dtype=torch.int32, device="cuda")
         its = torch.zeros(16, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()  # the decoder runs on the code's own stream
         st = cb.lib().cb_decode_device(g._h, C.c_void_p(flat.data_ptr() + 4 * off), 16, C.c_void_p(bits.data_ptr()),
                                        None, C.c_void_p(its.data_ptr()), None)
         assert st == 0
         torch.cuda.synchronize()
         outs.append((bits.cpu(), its.cpu()))
     assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
-    assert torch.equal(outs[0][0].numpy().view("u4").astype("u4")[:, :1], outs[0][0].numpy().view("u4")[:, :1])
+    # and they are the host-buffer decoder's
+    ref_bits, _, ref_it = g.decode_full(llr)
+    assert np.array_equal(outs[0][1].numpy(), ref_it)
+    got = np.unpackbits(outs[0][0].numpy().view(np.uint8), axis=1, bitorder="little")[:, :8448]
+    assert np.array_equal(got, ref_bits)
