@@ -36,12 +36,6 @@ __device__ __forceinline__ double infinity<double>() { return __longlong_as_doub
 template <>
 __device__ __forceinline__ float infinity<float>() { return __int_as_float(0x7f800000); }
 
-__device__ __forceinline__ int lifted_col(uint32_t entry, int r, int z) {
-  int c = r + (int)(entry & 0xffffu);
-  c -= (c >= z) ? z : 0;
-  return (int)(entry >> 16) * z + c;
-}
-
 // ---- syndrome test on packed hard decisions
 // hd holds, per base column j, the hard decisions of its Z bits packed 32 per word
 // (ceil(Z/32) words, then one zero word).  The parity of the 32 lifted rows
@@ -166,20 +160,9 @@ __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t*
   }
 }
 
-// Byte offset in post of edge e's variable for lifted row r, from the packed entry
-// (base column << 16 | shift).
-struct EdgeAddrPacked {
-  const uint32_t* ent;
-  int r, z;
-  __device__ __forceinline__ int operator()(int e) const {
-    const uint32_t en = ent[e];
-    unsigned c = (unsigned)r + (en & 0xffffu);
-    unsigned cm = c - (unsigned)z;
-    return 4 * ((int)(en >> 16) * z + (int)min(c, cm));
-  }
-};
-// The same from the per-entry table {4 (col Z + shift), Z - shift} of DevCode::eaddr:
-// 4 (col Z + (r + shift) mod Z) = 4 r + x, less 4 Z when r >= Z - shift.
+// Byte offset in post of edge e's variable for lifted row r, from the per-entry table
+// {4 (col Z + shift), Z - shift} of DevCode::eaddr: 4 (col Z + (r + shift) mod Z) = 4 r + x,
+// less 4 Z when r >= Z - shift.
 struct EdgeAddrTable {
   const uint2* tab;
   int r, r4, z4;
@@ -375,15 +358,10 @@ __device__ __forceinline__ void row_dispatch_lean(int d, float* post, const Addr
   }
 }
 
+// the row update of the f64 decoder (f32 rows take row_dispatch_lean)
 template <typename T>
 __device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent, int r, int z, T a1, T a2,
                                              uint32_t mt, int rule, T alpha, T& n1, T& n2, uint32_t& nm) {
-#ifndef CB_F32_CLASSIC_ROWS
-  if constexpr (sizeof(T) == 4) {
-    row_dispatch_lean(d, post, EdgeAddrPacked{ent, r, z}, a1, a2, mt, rule, alpha, n1, n2, nm);
-    return;
-  }
-#endif
   switch (d) {
     case 3: row_update<T, 3>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
     case 4: row_update<T, 4>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
