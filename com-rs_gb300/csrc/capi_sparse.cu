@@ -17,8 +17,9 @@ namespace {
 thread_local std::string g_ldpc_thread_error;
 
 // shared memory the edge messages may take before they move to global slots: keeps
-// two CTAs resident per SM
+// two CTAs resident per SM; and the posteriors, before they move there too
 constexpr size_t kSmemMsgBudget = 100 * 1024;
+constexpr size_t kSmemPostBudget = 200 * 1024;
 
 }  // namespace
 
@@ -35,6 +36,7 @@ struct cb_ldpc {
   int grid = 0, threads = 0;
   size_t smem = 0;
   bool msgs_in_smem = false;
+  bool post_in_smem = true;
   bool warp_rows = false;
   void* kernel = nullptr;
   cudaStream_t stream = nullptr;
@@ -115,15 +117,22 @@ cb_status ensure_device(cb_ldpc* c) {
   const size_t post_bytes = (size_t)h.n * elem(c);
   const size_t msg_bytes = (size_t)2 * h.edges * elem(c);
   c->msgs_in_smem = post_bytes + msg_bytes <= kSmemMsgBudget;
-  c->smem = (post_bytes + (c->msgs_in_smem ? msg_bytes : 0) + 15) & ~(size_t)15;
-  if (c->smem > 227 * 1024) return lfail(c, CB_ERR_CONFIG, "the posteriors of this code do not fit in shared memory");
+  c->post_in_smem = post_bytes <= kSmemPostBudget;
+  c->smem = c->msgs_in_smem ? ((post_bytes + msg_bytes + 15) & ~(size_t)15)
+                            : (c->post_in_smem ? ((post_bytes + 15) & ~(size_t)15) : 0);
+  const size_t slot_bytes = msg_bytes + (c->post_in_smem ? 0 : post_bytes);
   c->kernel = cbk::sparse_kernel_ptr(c->precision == CB_F64 ? 0 : 1, c->rule, c->layered != 0);
   LDPC_CUDA(c, cudaFuncSetAttribute(c->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
   int per_sm = 0, sms = 0;
   LDPC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c->kernel, c->threads, c->smem));
   LDPC_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
   c->grid = std::max(1, per_sm * sms);
-  if (!c->msgs_in_smem) LDPC_CUDA(c, cudaMalloc(&c->d_slots, (size_t)c->grid * msg_bytes));
+  if (!c->msgs_in_smem) {
+    // the global slots of all resident CTAs, at most 2 GB
+    const int cap = (int)std::max<size_t>(1, ((size_t)2 << 30) / slot_bytes);
+    c->grid = std::min(c->grid, cap);
+    LDPC_CUDA(c, cudaMalloc(&c->d_slots, (size_t)c->grid * slot_bytes));
+  }
   c->dev_ready = true;
   return CB_OK;
 }
@@ -136,6 +145,7 @@ cb_status decode_impl(cb_ldpc* c, const T* llr, int64_t n, T* post, int32_t* ite
   a.alpha = c->alpha;
   a.max_iterations = c->max_iterations;
   a.msgs_in_smem = c->msgs_in_smem ? 1 : 0;
+  a.post_in_smem = c->post_in_smem ? 1 : 0;
   a.warp_rows = c->warp_rows ? 1 : 0;
   a.llr = llr;
   a.n_frames = n;

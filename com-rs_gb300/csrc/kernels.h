@@ -187,13 +187,14 @@ struct SparseArgs {
   SparseDev code;
   double alpha;  // NMS scale or OMS offset
   int32_t max_iterations;
+  int32_t post_in_smem;  // 1: the posteriors live in shared memory, else in `slots` too
   int32_t msgs_in_smem;  // 1: the edge messages live in shared memory, else in `slots`
   int32_t warp_rows;     // layered: one warp per row (levels of few rows), else one thread
   const T* llr;          // [n_frames][n]
   int64_t n_frames;
   T* post_out;           // [n_frames][n] (nullable)
   int32_t* iters_out;    // [n_frames] (nullable)
-  T* slots;              // [grid][2][edges] when !msgs_in_smem
+  T* slots;              // [grid][2 edges (+ n when !post_in_smem)] when !msgs_in_smem
   unsigned long long* work_counter;
 };
 // the kernel of a precision (0: f64, 1: f32), rule and schedule

@@ -4,9 +4,10 @@
 // or the lifted rows of a 5G NR code).
 //
 // One CTA decodes one codeword at a time (a persistent grid with an atomic work
-// counter).  The posteriors sit in shared memory; the check-to-variable messages, one
-// per edge as in the reference, sit in shared memory when they fit and otherwise in the
-// CTA's slot of a global buffer.
+// counter).  The posteriors sit in shared memory, and the check-to-variable messages,
+// one per edge as in the reference, too when they fit; what does not fit (the messages
+// of large codes, and the posteriors of the largest, e.g. DVB-S2 normal frames) sits in
+// the CTA's slot of a global buffer.
 //
 //   * Layered: the rows run level by level (the level schedule of sparse_host.h), one
 //     thread per row of the level, a barrier between levels.  This is the reference's
@@ -233,15 +234,18 @@ __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ Spa
   extern __shared__ __align__(16) unsigned char smem[];
   const SparseDev& c = a.code;
   const int tid = threadIdx.x, nt = blockDim.x;
-  T* post = reinterpret_cast<T*>(smem);
+  T* post;
   T* msg;
   T* aux;
   if (a.msgs_in_smem) {
+    post = reinterpret_cast<T*>(smem);
     msg = post + c.n;
     aux = msg + c.edges;
   } else {
-    msg = a.slots + (size_t)blockIdx.x * 2 * c.edges;
+    const size_t per = (size_t)2 * c.edges + (a.post_in_smem ? 0 : (size_t)c.n);
+    msg = a.slots + (size_t)blockIdx.x * per;
     aux = msg + c.edges;
+    post = a.post_in_smem ? reinterpret_cast<T*>(smem) : aux + c.edges;
   }
   const T alpha = (T)a.alpha;
   __shared__ long long s_cw;

@@ -190,3 +190,24 @@ def test_dvbs2_short_rate_half_overlaps_aff3ct(cb):
         assert not (a_hi < c_lo or c_hi < a_lo), (p["ebn0_db"], fe / nf, p["fer"])
         checked += 1
     assert checked == (5 if full else 3)
+
+
+@pytest.mark.parametrize("rule", ["normalized_min_sum", "sum_product"])
+def test_dvbs2_normal_frame_decodes_with_posteriors_in_global_memory(cb, rule):
+    # n = 64 800: the f64 posteriors (518 KB) exceed shared memory and live in the CTAs'
+    # global slots with the messages.  Above the decoding threshold every all-zero frame
+    # decodes, in more than one iteration, and a second run gives the same posteriors.
+    code = cb.Dvbs2Ldpc("normal", "1/2", rule=rule, alpha=0.75, max_iterations=30)
+    assert code.info()["n"] == 64800
+    rng = np.random.default_rng(5)
+    rate = 0.5
+    # above the threshold of each rule (the normalised min-sum needs about 0.2 dB more,
+    # fec.rs:262-263)
+    ebn0 = 1.6 if rule == "sum_product" else 2.3
+    noise_var = 1.0 / (2.0 * rate * 10 ** (ebn0 / 10))
+    y = 1.0 + np.sqrt(noise_var) * rng.standard_normal((8, 64800))
+    llr = 2.0 * y / noise_var
+    post, its = code.decode_llr(llr)
+    assert (post > 0).all() and (its < 30).all() and (its > 1).all()
+    post2, its2 = code.decode_llr(llr)
+    assert np.array_equal(post.view(np.uint64), post2.view(np.uint64)) and np.array_equal(its, its2)
