@@ -82,8 +82,34 @@ cb_status ensure_device(cb_ldpc* c) {
   const cbh::SparseCode& h = c->host;
   LDPC_CUDA(c, cudaSetDevice(c->device));
   if (!c->stream) LDPC_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  // the launch shape decides the message layout: a thread per row with messages in
+  // global memory takes the transposed one
+  c->warp_rows = c->layered && h.max_level_rows <= 8 && h.max_row_degree <= 128;
+  const size_t post_bytes = (size_t)h.n * elem(c);
+  const size_t msg_bytes_rm = (size_t)2 * h.edges * elem(c);
+  c->msgs_in_smem = post_bytes + msg_bytes_rm <= kSmemMsgBudget;
+  c->post_in_smem = post_bytes <= kSmemPostBudget;
+  const bool transposed = !c->msgs_in_smem && !c->warp_rows;
+  std::vector<int32_t> tvars, col_slots;
+  if (transposed) {
+    // position of every row in the schedule: its place in the level order (layered) or
+    // its index (flooding)
+    std::vector<int32_t> pos(h.m);
+    for (int i = 0; i < h.m; i++) pos[c->layered ? h.level_rows[i] : i] = i;
+    const size_t nslot = (size_t)h.max_row_degree * h.m;
+    tvars.assign(nslot, 0);
+    std::vector<int32_t> slot_of_edge(h.edges);
+    for (int r = 0; r < h.m; r++)
+      for (int e = h.row_start[r]; e < h.row_start[r + 1]; e++) {
+        const size_t sl = (size_t)(e - h.row_start[r]) * h.m + pos[r];
+        tvars[sl] = h.vars[e];
+        slot_of_edge[e] = (int32_t)sl;
+      }
+    col_slots.resize(h.edges);
+    for (int k = 0; k < h.edges; k++) col_slots[k] = slot_of_edge[h.col_edges[k]];
+  }
   const size_t words = h.row_start.size() + h.vars.size() + h.col_start.size() + h.col_edges.size() +
-                       h.level_start.size() + h.level_rows.size();
+                       h.level_start.size() + h.level_rows.size() + tvars.size();
   LDPC_CUDA(c, cudaMalloc(&c->d_tables, words * 4));
   int32_t* p = c->d_tables;
   auto put = [&](const std::vector<int32_t>& v, const int32_t*& dst) -> cudaError_t {
@@ -100,24 +126,23 @@ cb_status ensure_device(cb_ldpc* c) {
   LDPC_CUDA(c, put(h.row_start, d.row_start));
   LDPC_CUDA(c, put(h.vars, d.vars));
   LDPC_CUDA(c, put(h.col_start, d.col_start));
-  LDPC_CUDA(c, put(h.col_edges, d.col_edges));
+  LDPC_CUDA(c, put(transposed ? col_slots : h.col_edges, d.col_edges));
   LDPC_CUDA(c, put(h.level_start, d.level_start));
   LDPC_CUDA(c, put(h.level_rows, d.level_rows));
+  d.tvars = nullptr;
+  if (transposed) LDPC_CUDA(c, put(tvars, d.tvars));
+  d.slots = transposed ? (int32_t)((size_t)h.max_row_degree * h.m) : h.edges;
   LDPC_CUDA(c, cudaMalloc(&c->d_counter, sizeof(unsigned long long)));
   // threads: a level's rows (layered), one warp per row when the levels hold few rows
   // (at most 8) of at most 128 edges, else a thread per row; a share of the rows and
   // variables (flooding)
-  c->warp_rows = c->layered && h.max_level_rows <= 8 && h.max_row_degree <= 128;
   if (c->warp_rows) {
     c->threads = 32 * h.max_level_rows;
   } else {
     const int want = c->layered ? h.max_level_rows : std::max(h.m, h.n) / 4;
     c->threads = std::min(512, std::max(64, (want + 31) / 32 * 32));
   }
-  const size_t post_bytes = (size_t)h.n * elem(c);
-  const size_t msg_bytes = (size_t)2 * h.edges * elem(c);
-  c->msgs_in_smem = post_bytes + msg_bytes <= kSmemMsgBudget;
-  c->post_in_smem = post_bytes <= kSmemPostBudget;
+  const size_t msg_bytes = (size_t)2 * d.slots * elem(c);
   c->smem = c->msgs_in_smem ? ((post_bytes + msg_bytes + 15) & ~(size_t)15)
                             : (c->post_in_smem ? ((post_bytes + 15) & ~(size_t)15) : 0);
   const size_t slot_bytes = msg_bytes + (c->post_in_smem ? 0 : post_bytes);

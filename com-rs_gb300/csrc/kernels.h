@@ -181,6 +181,11 @@ struct SparseDev {
   const int32_t* col_edges;    // edges, per variable in row order
   const int32_t* level_start;  // levels + 1
   const int32_t* level_rows;   // m
+  // transposed layout of the messages (global-memory messages, a thread per row): edge k
+  // of the row at schedule position p is slot k m + p, and tvars[k m + p] its variable;
+  // col_edges then holds slots.  Null: the row-major layout of the edges.
+  const int32_t* tvars;        // max row degree x m
+  int32_t slots;               // message slots of one buffer: edges, or max row degree x m
 };
 template <typename T>
 struct SparseArgs {

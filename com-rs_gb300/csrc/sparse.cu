@@ -52,21 +52,33 @@ __device__ __forceinline__ T clamp_t(T x, T lo, T hi) {
 // each pass, always to the same value).  Layered: the outputs go to msg (replacing the
 // old messages after they are read) and to post; flooding: to out only.  aux holds the
 // prefix products of the sum-product rule.
+// Edge k of a row: its message slot and its variable, in the row-major layout (slot
+// e0 + k) or the transposed one (slot k m + pos, consecutive for consecutive threads).
+struct EdgeSlots {
+  const int32_t* vars;
+  int base, stride;
+  __device__ __forceinline__ int slot(int k) const { return base + k * stride; }
+  __device__ __forceinline__ int var(int k) const { return vars[slot(k)]; }
+};
+
 template <typename T, int RULE, bool LAYERED>
-__device__ __forceinline__ void check_row(const SparseDev& c, int row, T* post, T* msg, T* out, T* aux, T alpha) {
-  const int e0 = c.row_start[row], e1 = c.row_start[row + 1];
+__device__ __forceinline__ void check_row(const SparseDev& c, int row, int pos, T* post, T* msg, T* out, T* aux,
+                                          T alpha) {
+  const int d = c.row_start[row + 1] - c.row_start[row];
+  const EdgeSlots es = c.tvars ? EdgeSlots{c.tvars, pos, c.m} : EdgeSlots{c.vars, c.row_start[row], 1};
   if (RULE == cbd::RULE_SUM_PRODUCT) {
     // the product of the other tanh(L/2) by prefix and suffix products
     T prefix = (T)1;
-    for (int e = e0; e < e1; e++) {
-      const T l = sub_rn(post[c.vars[e]], msg[e]);
+    for (int k = 0; k < d; k++) {
+      const int e = es.slot(k);
+      const T l = sub_rn(post[es.var(k)], msg[e]);
       const T t = tanh_t(mul_rn(l, (T)0.5));
       aux[e] = prefix;
       prefix = mul_rn(prefix, t);
     }
     T suffix = (T)1;
-    for (int e = e1 - 1; e >= e0; e--) {
-      const int v = c.vars[e];
+    for (int k = d - 1; k >= 0; k--) {
+      const int e = es.slot(k), v = es.var(k);
       const T l = sub_rn(post[v], msg[e]);
       const T t = tanh_t(mul_rn(l, (T)0.5));
       const T p = mul_rn(aux[e], suffix);
@@ -82,8 +94,8 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, T* post, 
   } else {
     int neg = 0, i1 = 0;
     T m1 = infinity<T>(), m2 = infinity<T>();
-    for (int e = e0, i = 0; e < e1; e++, i++) {
-      const T l = sub_rn(post[c.vars[e]], msg[e]);
+    for (int i = 0; i < d; i++) {
+      const T l = sub_rn(post[es.var(i)], msg[es.slot(i)]);
       neg ^= (int)(l < (T)0);
       const T a = fabs(l);
       if (a < m1) {
@@ -95,8 +107,8 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, T* post, 
       }
     }
     const T sign = neg ? (T)-1 : (T)1;
-    for (int e = e0, i = 0; e < e1; e++, i++) {
-      const int v = c.vars[e];
+    for (int i = 0; i < d; i++) {
+      const int e = es.slot(i), v = es.var(i);
       const T l = sub_rn(post[v], msg[e]);
       const T s = mul_rn(sign, l < (T)0 ? (T)-1 : (T)1);
       T mag = i == i1 ? m2 : m1;
@@ -240,12 +252,12 @@ __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ Spa
   if (a.msgs_in_smem) {
     post = reinterpret_cast<T*>(smem);
     msg = post + c.n;
-    aux = msg + c.edges;
+    aux = msg + c.slots;
   } else {
-    const size_t per = (size_t)2 * c.edges + (a.post_in_smem ? 0 : (size_t)c.n);
+    const size_t per = (size_t)2 * c.slots + (a.post_in_smem ? 0 : (size_t)c.n);
     msg = a.slots + (size_t)blockIdx.x * per;
-    aux = msg + c.edges;
-    post = a.post_in_smem ? reinterpret_cast<T*>(smem) : aux + c.edges;
+    aux = msg + c.slots;
+    post = a.post_in_smem ? reinterpret_cast<T*>(smem) : aux + c.slots;
   }
   const T alpha = (T)a.alpha;
   __shared__ long long s_cw;
@@ -256,7 +268,7 @@ __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ Spa
     if (cw >= a.n_frames) break;
     const T* llr = a.llr + (size_t)cw * c.n;
     for (int v = tid; v < c.n; v += nt) post[v] = llr[v];
-    for (int e = tid; e < c.edges; e += nt) {
+    for (int e = tid; e < c.slots; e += nt) {
       msg[e] = (T)0;
       aux[e] = (T)0;
     }
@@ -277,12 +289,13 @@ __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ Spa
         } else if (LAYERED) {
           for (int L = 0; L < c.levels; L++) {
             const int r0 = c.level_start[L], r1 = c.level_start[L + 1];
-            for (int i = r0 + tid; i < r1; i += nt) check_row<T, RULE, true>(c, c.level_rows[i], post, msg, nullptr, aux, alpha);
+            for (int i = r0 + tid; i < r1; i += nt)
+              check_row<T, RULE, true>(c, c.level_rows[i], i, post, msg, nullptr, aux, alpha);
             __syncthreads();
           }
         } else {
           // the sum-product rule keeps its prefix products in `next`, where its outputs go
-          for (int r = tid; r < c.m; r += nt) check_row<T, RULE, false>(c, r, post, cur, next, next, alpha);
+          for (int r = tid; r < c.m; r += nt) check_row<T, RULE, false>(c, r, r, post, cur, next, next, alpha);
           __syncthreads();
           for (int v = tid; v < c.n; v += nt) {
             T s = llr[v];
