@@ -156,15 +156,12 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
             }
           }
         }
-        // the state of a layer is prefetched one layer ahead
-        T a1 = (T)0, a2 = (T)0;
-        uint32_t mt = 0;
-        if (iter > 1 && active) st.load(c.layer_order[0] * z + tid, a1, a2, mt);
+        // the row's state from the previous iteration (L2-resident: loaded where it is used)
         for (int q = 0; q < c.rows_n; q++) {
           const int L = c.layer_order[q];
-          T p1 = (T)0, p2 = (T)0;
-          uint32_t pm = 0;
-          if (iter > 1 && active && q + 1 < c.rows_n) st.load(c.layer_order[q + 1] * z + tid, p1, p2, pm);
+          T a1 = (T)0, a2 = (T)0;
+          uint32_t mt = 0;
+          if (iter > 1 && active) st.load(L * z + tid, a1, a2, mt);
           if (active) {
             const int s0 = c.layer_start[L];
             const int d = c.layer_start[L + 1] - s0;
@@ -181,9 +178,6 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
               row_dispatch<T>(d, post, c.entry + s0, tid, z, a1, a2, mt, rule, alpha, n1, n2, nm);
             st.store(L * z + tid, n1, n2, nm);
           }
-          a1 = p1;
-          a2 = p2;
-          mt = pm;
           if (c.level_end[q]) __syncthreads();
         }
         if (!some_check_fails(post, hd, s_ent, s_lstart, c.rows_n, ncol, z, tid, nt)) {
