@@ -106,41 +106,22 @@ __device__ void decode_item(const MixDecodeArgs& a, const MixItem& it, unsigned 
   if (slot_check_fails(post, hd, s_ent, s_lstart, rows_n, ncol, z, lt, nt, bar, flag)) {
     iters = a.max_it;
     for (int iter = 1; iter <= a.max_it; iter++) {
-      float a1[RHO], a2[RHO];
-      uint32_t mt[RHO];
-#pragma unroll
-      for (int q = 0; q < RHO; q++) {
-        a1[q] = a2[q] = 0.f;
-        mt[q] = 0u;
-        const int r = lt + q * nt;
-        if (iter > 1 && r < z) st.load(s_order[0] * z + r, a1[q], a2[q], mt[q]);
-      }
-      // the base rows by levels, as decode.cu runs them
+      // the base rows by levels, as decode.cu runs them; each row's state is loaded where
+      // it is used
       for (int k = 0; k < rows_n; k++) {
         const int L = s_order[k];
-        float p1[RHO], p2[RHO];
-        uint32_t pm[RHO];
-#pragma unroll
-        for (int q = 0; q < RHO; q++) {
-          p1[q] = p2[q] = 0.f;
-          pm[q] = 0u;
-          const int r = lt + q * nt;
-          if (iter > 1 && r < z && k + 1 < rows_n) st.load(s_order[k + 1] * z + r, p1[q], p2[q], pm[q]);
-        }
         const int s0 = s_lstart[L], d = s_lstart[L + 1] - s0;
 #pragma unroll
         for (int q = 0; q < RHO; q++) {
           const int r = lt + q * nt;
           if (r < z) {
-            float n1, n2;
-            uint32_t nm;
-            row_dispatch_lean(d, post, EdgeAddrTable{s_addr + s0, r, 4 * r, 4 * z}, a1[q], a2[q], mt[q], a.rule,
-                              a.alpha, n1, n2, nm);
+            float a1 = 0.f, a2 = 0.f, n1, n2;
+            uint32_t mt = 0u, nm;
+            if (iter > 1) st.load(L * z + r, a1, a2, mt);
+            row_dispatch_lean(d, post, EdgeAddrTable{s_addr + s0, r, 4 * r, 4 * z}, a1, a2, mt, a.rule, a.alpha, n1,
+                              n2, nm);
             st.store(L * z + r, n1, n2, nm);
           }
-          a1[q] = p1[q];
-          a2[q] = p2[q];
-          mt[q] = pm[q];
         }
         if (s_end[k]) slot_sync(bar, nt);
       }
