@@ -19,6 +19,8 @@ CODES = [
     dict(k=1000, e=1504, m=256),
     dict(k=8448, e=25344, bg=1, z=384, m=16),       # benchmark config 2
     dict(k=8448, e=16896, bg=1, z=384, m=64),       # benchmark config 5
+    dict(k=60, e=1000, rv=1, qm=2, m=4),            # repeated bits (E > N_cb)
+    dict(k=1000, e=1500, rv=3, qm=6, m=64),         # rv 3, bit interleaver of 6 rows
 ]
 
 
