@@ -176,3 +176,27 @@ def test_decode_device_accepts_a_buffer_of_any_alignment(cb):
     assert np.array_equal(outs[0][1].numpy(), ref_it)
     got = np.unpackbits(outs[0][0].numpy().view(np.uint8), axis=1, bitorder="little")[:, :8448]
     assert np.array_equal(got, ref_bits)
+
+
+def test_concurrent_callers_on_one_code_object(cb):
+    # calls on one code object are serialised by its mutex: four host threads decoding
+    # through the same object get what one thread gets
+    import threading
+
+    g = cb.NrLdpc(520, 1040, base_graph=2, lifting_size=52, precision="f32")
+    llr, _ = g.generate_frames(7, "threads", 0, 0, 4 * 256, 1.0, 4)
+    want = [g.decode_full(llr[i * 256:(i + 1) * 256]) for i in range(4)]
+    got = [None] * 4
+
+    def work(i):
+        for _ in range(3):
+            got[i] = g.decode_full(llr[i * 256:(i + 1) * 256])
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for (wb, wa, wi), (gb, ga, gi) in zip(want, got):
+        assert np.array_equal(wb, gb) and np.array_equal(wi, gi)
+        assert np.array_equal(wa.view(np.uint32), ga.view(np.uint32))
