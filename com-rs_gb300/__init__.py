@@ -96,6 +96,12 @@ SYMBOLS = [
     ("cb_ldpc_levels", _i32, [_vp, _vp, _vp]),
     ("cb_ldpc_decode", _i32, [_vp, _vp, _i64, _vp, _vp]),
     ("cb_ldpc_decode_device", _i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    ("cb_ldpc_set_decoder", _i32, [_vp, _i32, _dbl, _i32, _i32]),
+    ("cb_ldpc_girth", _i32, [_vp, _vp]),
+    ("cb_ldpc_set_encoder", _i32, [_vp, _i32, _vp, _vp]),
+    ("cb_ldpc_encode", _i32, [_vp, _vp, _i64, _vp]),
+    ("cb_ldpc_encode_device", _i32, [_vp, _vp, _i64, _vp, _vp]),
+    ("cb_ldpc_peg", _i32, [_i32, _i32, _i32, _u64, _vp, _vp]),
 ]
 
 _lib = None

@@ -1,6 +1,8 @@
 // The C ABI of generic sparse LDPC codes (cb_ldpc_* of include/comrs_gb300.h):
 // LdpcCode::decode_llr (crates/com-fec/src/ldpc.rs:497-505) on the GPU for any
-// parity-check matrix, with the decoder settings of LdpcDecoder (ldpc.rs:165-172).
+// parity-check matrix, with the decoder settings of LdpcDecoder (ldpc.rs:165-172);
+// LdpcCode::encode_block (ldpc.rs:753-791) on the GPU with the encoder of from_rows or
+// accumulate; and the host-side constructions (progressive edge growth, girth).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,6 +48,14 @@ struct cb_ldpc {
   size_t post_cap = 0;
   int32_t* d_iters = nullptr;
   size_t iters_cap = 0;
+  // the systematic encoder: host tables, their device copy, staging buffers
+  cbh::SparseEncoder enc;
+  bool enc_ready = false;
+  int32_t* d_enc = nullptr;
+  void* d_info = nullptr;
+  size_t info_cap = 0;
+  void* d_coded = nullptr;
+  size_t coded_cap = 0;
   std::string err;
 };
 
@@ -77,11 +87,31 @@ cudaError_t grow_buf(void** ptr, size_t& cap, size_t bytes) {
 size_t elem(const cb_ldpc* c) { return c->precision == CB_F64 ? 8 : 4; }
 
 // device tables, launch shape and message storage, on first use
+cb_status ensure_stream(cb_ldpc* c) {
+  LDPC_CUDA(c, cudaSetDevice(c->device));
+  if (!c->stream) LDPC_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  return CB_OK;
+}
+
+// the decoder's device tables and message slots (the stream and the staging buffers stay)
+void release_decoder(cb_ldpc* c) {
+  if (!c->dev_ready) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->d_tables);
+  cudaFree(c->d_counter);
+  cudaFree(c->d_slots);
+  c->d_tables = nullptr;
+  c->d_counter = nullptr;
+  c->d_slots = nullptr;
+  c->dev = cbk::SparseDev{};
+  c->dev_ready = false;
+}
+
 cb_status ensure_device(cb_ldpc* c) {
   if (c->dev_ready) return CB_OK;
   const cbh::SparseCode& h = c->host;
-  LDPC_CUDA(c, cudaSetDevice(c->device));
-  if (!c->stream) LDPC_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  if (cb_status st = ensure_stream(c)) return st;
   // the launch shape decides the message layout: a thread per row with messages in
   // global memory takes the transposed one
   c->warp_rows = c->layered && h.max_level_rows <= 8 && h.max_row_degree <= 128;
@@ -184,6 +214,77 @@ cb_status decode_impl(cb_ldpc* c, const T* llr, int64_t n, T* post, int32_t* ite
   return CB_OK;
 }
 
+// shared memory the encoders may take per CTA
+constexpr size_t kEncodeSmemLimit = 200 * 1024;
+
+// the encoder's tables on the device: sums: info positions, pivots, packed rows;
+// accumulate: the rows of H
+cb_status ensure_encoder(cb_ldpc* c) {
+  if (c->enc.kind == cbh::kEncoderNone)
+    return lfail(c, CB_ERR_CONFIG, "the code has no encoder: call cb_ldpc_set_encoder first");
+  if (c->enc_ready) return CB_OK;
+  if (cb_status st = ensure_stream(c)) return st;
+  const cbh::SparseEncoder& e = c->enc;
+  const cbh::SparseCode& h = c->host;
+  std::vector<int32_t> tab;
+  if (e.kind == cbh::kEncoderSums) {
+    if (cbk::sums_encode_smem(e.words) > kEncodeSmemLimit)
+      return lfail(c, CB_ERR_CONFIG, "k = " + std::to_string(e.k) + " is too large for the encoder");
+    tab.insert(tab.end(), e.info.begin(), e.info.end());
+    tab.insert(tab.end(), e.pivots.begin(), e.pivots.end());
+    for (uint32_t w : e.pmat) tab.push_back((int32_t)w);
+  } else {
+    if (cbk::accumulate_encode_smem(e.k, h.m) > kEncodeSmemLimit)
+      return lfail(c, CB_ERR_CONFIG, "n = " + std::to_string(h.n) + " is too large for the encoder");
+    tab.insert(tab.end(), h.row_start.begin(), h.row_start.end());
+    tab.insert(tab.end(), h.vars.begin(), h.vars.end());
+  }
+  LDPC_CUDA(c, cudaMalloc(&c->d_enc, std::max<size_t>(1, tab.size()) * 4));
+  LDPC_CUDA(c, cudaMemcpy(c->d_enc, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
+  c->enc_ready = true;
+  return CB_OK;
+}
+
+cb_status encode_impl(cb_ldpc* c, const uint8_t* info, int64_t n, uint8_t* coded, cudaStream_t s) {
+  if (n == 0) return CB_OK;
+  const cbh::SparseEncoder& e = c->enc;
+  const cbh::SparseCode& h = c->host;
+  if (e.kind == cbh::kEncoderSums) {
+    cbk::SumsEncodeArgs a;
+    a.info = info;
+    a.coded = coded;
+    a.n_frames = n;
+    a.k = e.k;
+    a.n = h.n;
+    a.rank = (int32_t)e.pivots.size();
+    a.words = e.words;
+    a.info_pos = c->d_enc;
+    a.pivots = c->d_enc + e.k;
+    a.pmat = reinterpret_cast<const uint32_t*>(c->d_enc + e.k + e.pivots.size());
+    LDPC_CUDA(c, cbk::launch_sums_encode(a, s));
+  } else {
+    cbk::AccumulateEncodeArgs a;
+    a.info = info;
+    a.coded = coded;
+    a.n_frames = n;
+    a.k = e.k;
+    a.n = h.n;
+    a.m = h.m;
+    a.row_start = c->d_enc;
+    a.vars = c->d_enc + h.m + 1;
+    LDPC_CUDA(c, cbk::launch_accumulate_encode(a, s));
+  }
+  return CB_OK;
+}
+
+cb_status check_decoder_settings(int32_t rule, double alpha, int32_t max_iterations) {
+  if (rule != CB_RULE_SUM_PRODUCT && rule != CB_RULE_NMS && rule != CB_RULE_OMS)
+    return lfail(nullptr, CB_ERR_CONFIG, "rule must be sum-product, normalised or offset min-sum");
+  if (max_iterations < 0) return lfail(nullptr, CB_ERR_CONFIG, "max_iterations must be >= 0");
+  if (!std::isfinite(alpha)) return lfail(nullptr, CB_ERR_CONFIG, "alpha must be finite");
+  return CB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -193,11 +294,8 @@ cb_status cb_ldpc_create(int32_t n, int32_t m, const int32_t* row_start, const i
                          cb_ldpc** out) {
   if (!out) return lfail(nullptr, CB_ERR_CONFIG, "null output pointer");
   *out = nullptr;
-  if (rule != CB_RULE_SUM_PRODUCT && rule != CB_RULE_NMS && rule != CB_RULE_OMS)
-    return lfail(nullptr, CB_ERR_CONFIG, "rule must be sum-product, normalised or offset min-sum");
-  if (max_iterations < 0) return lfail(nullptr, CB_ERR_CONFIG, "max_iterations must be >= 0");
+  if (cb_status st = check_decoder_settings(rule, alpha, max_iterations)) return st;
   if (precision != CB_F64 && precision != CB_F32) return lfail(nullptr, CB_ERR_CONFIG, "precision must be f64 or f32");
-  if (!std::isfinite(alpha)) return lfail(nullptr, CB_ERR_CONFIG, "alpha must be finite");
   cb_ldpc* c = new cb_ldpc;
   std::string err;
   if (!cbh::build_sparse_code(n, m, row_start, vars, c->host, err)) {
@@ -216,7 +314,7 @@ cb_status cb_ldpc_create(int32_t n, int32_t m, const int32_t* row_start, const i
 
 void cb_ldpc_destroy(cb_ldpc* c) {
   if (!c) return;
-  if (c->dev_ready || c->stream) {
+  if (c->dev_ready || c->stream || c->enc_ready) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->d_tables);
@@ -225,6 +323,9 @@ void cb_ldpc_destroy(cb_ldpc* c) {
     cudaFree(c->d_llr);
     cudaFree(c->d_post);
     cudaFree(c->d_iters);
+    cudaFree(c->d_enc);
+    cudaFree(c->d_info);
+    cudaFree(c->d_coded);
     if (c->stream) cudaStreamDestroy(c->stream);
   }
   delete c;
@@ -288,6 +389,97 @@ cb_status cb_ldpc_decode(cb_ldpc* c, const void* llr, int64_t n_frames, void* po
     if (iterations)
       LDPC_CUDA(c, cudaMemcpyAsync(iterations + f0, c->d_iters, k * 4, cudaMemcpyDeviceToHost, c->stream));
     LDPC_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return CB_OK;
+}
+
+cb_status cb_ldpc_set_decoder(cb_ldpc* c, int32_t rule, double alpha, int32_t layered, int32_t max_iterations) {
+  if (!c) return lfail(nullptr, CB_ERR_CONFIG, "null code");
+  if (cb_status st = check_decoder_settings(rule, alpha, max_iterations)) {
+    c->err = g_ldpc_thread_error;
+    return st;
+  }
+  std::lock_guard<std::mutex> lock(c->mu);
+  // the kernel and the message layout follow the rule and the schedule
+  if (rule != c->rule || (layered ? 1 : 0) != c->layered) release_decoder(c);
+  c->rule = rule;
+  c->alpha = alpha;
+  c->layered = layered ? 1 : 0;
+  c->max_iterations = max_iterations;
+  return CB_OK;
+}
+
+cb_status cb_ldpc_girth(const cb_ldpc* c, int32_t* girth) {
+  if (!c || !girth) return lfail(nullptr, CB_ERR_CONFIG, "null argument");
+  *girth = cbh::girth(c->host);
+  return CB_OK;
+}
+
+cb_status cb_ldpc_set_encoder(cb_ldpc* c, int32_t kind, int32_t* k, int32_t* info_positions) {
+  if (!c) return lfail(nullptr, CB_ERR_CONFIG, "null code");
+  if (kind != CB_ENC_SUMS && kind != CB_ENC_ACCUMULATE)
+    return lfail(c, CB_ERR_CONFIG, "the encoder must be CB_ENC_SUMS or CB_ENC_ACCUMULATE");
+  std::lock_guard<std::mutex> lock(c->mu);
+  if (c->enc.kind != kind) {
+    cbh::SparseEncoder enc;
+    std::string err;
+    const bool ok = kind == CB_ENC_SUMS ? cbh::reduce_sums(c->host, enc, err) : cbh::check_accumulate(c->host, enc, err);
+    if (!ok) return lfail(c, CB_ERR_CONFIG, err);
+    if (c->enc_ready) {
+      cudaSetDevice(c->device);
+      if (c->stream) cudaStreamSynchronize(c->stream);
+      cudaFree(c->d_enc);
+      c->d_enc = nullptr;
+      c->enc_ready = false;
+    }
+    c->enc = std::move(enc);
+  }
+  if (k) *k = c->enc.k;
+  if (info_positions) std::copy(c->enc.info.begin(), c->enc.info.end(), info_positions);
+  return CB_OK;
+}
+
+cb_status cb_ldpc_encode_device(cb_ldpc* c, const uint8_t* info, int64_t n_frames, uint8_t* coded, void* stream) {
+  if (!c) return lfail(nullptr, CB_ERR_CONFIG, "null code");
+  if (n_frames < 0) return lfail(c, CB_ERR_SHAPE, "n_frames must be >= 0");
+  if (n_frames > 0 && (!info || !coded)) return lfail(c, CB_ERR_SHAPE, "null information or coded bits");
+  std::lock_guard<std::mutex> lock(c->mu);
+  if (cb_status st = ensure_encoder(c)) return st;
+  return encode_impl(c, info, n_frames, coded, stream ? (cudaStream_t)stream : c->stream);
+}
+
+cb_status cb_ldpc_encode(cb_ldpc* c, const uint8_t* info, int64_t n_frames, uint8_t* coded) {
+  if (!c) return lfail(nullptr, CB_ERR_CONFIG, "null code");
+  if (n_frames < 0) return lfail(c, CB_ERR_SHAPE, "n_frames must be >= 0");
+  if (n_frames == 0) return CB_OK;
+  if (!info || !coded) return lfail(c, CB_ERR_SHAPE, "null information or coded bits");
+  std::lock_guard<std::mutex> lock(c->mu);
+  if (cb_status st = ensure_encoder(c)) return st;
+  const size_t k = (size_t)c->enc.k, n = (size_t)c->host.n;
+  // chunks of at most 1 GB of coded bits
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n_frames, (int64_t)(((size_t)1 << 30) / n)));
+  LDPC_CUDA(c, grow_buf(&c->d_info, c->info_cap, chunk * k));
+  LDPC_CUDA(c, grow_buf(&c->d_coded, c->coded_cap, chunk * n));
+  for (int64_t f0 = 0; f0 < n_frames; f0 += chunk) {
+    const int64_t cnt = std::min(chunk, n_frames - f0);
+    LDPC_CUDA(c, cudaMemcpyAsync(c->d_info, info + f0 * k, cnt * k, cudaMemcpyHostToDevice, c->stream));
+    if (cb_status st = encode_impl(c, (const uint8_t*)c->d_info, cnt, (uint8_t*)c->d_coded, c->stream)) return st;
+    LDPC_CUDA(c, cudaMemcpyAsync(coded + f0 * n, c->d_coded, cnt * n, cudaMemcpyDeviceToHost, c->stream));
+    LDPC_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return CB_OK;
+}
+
+cb_status cb_ldpc_peg(int32_t n, int32_t k, int32_t var_degree, uint64_t seed, int32_t* row_start, int32_t* vars) {
+  if (!row_start || !vars) return lfail(nullptr, CB_ERR_CONFIG, "null output pointer");
+  std::vector<std::vector<int32_t>> rows;
+  std::string err;
+  if (!cbh::peg_rows(n, k, var_degree, seed, rows, err)) return lfail(nullptr, CB_ERR_CONFIG, err);
+  int32_t e = 0;
+  row_start[0] = 0;
+  for (size_t r = 0; r < rows.size(); r++) {
+    for (int32_t v : rows[r]) vars[e++] = v;
+    row_start[r + 1] = e;
   }
   return CB_OK;
 }

@@ -6,61 +6,12 @@
 #include <cstdint>
 
 #include "code_host.h"
+#include "xoshiro.h"
 
 namespace cbd {
 
 // ---------------------------------------------------------------- xoshiro256**
-// crates/com-core/src/rng.rs:49-117, :270-278 (bit-identical)
-struct Xoshiro {
-  uint64_t s0, s1, s2, s3;
-};
-
-__host__ __device__ __forceinline__ uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
-
-__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t& st) {
-  st += 0x9E3779B97F4A7C15ull;
-  uint64_t z = st;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-
-__host__ __device__ __forceinline__ Xoshiro xoshiro_seed(uint64_t seed) {
-  Xoshiro r;
-  uint64_t st = seed;
-  r.s0 = splitmix64(st);
-  r.s1 = splitmix64(st);
-  r.s2 = splitmix64(st);
-  r.s3 = splitmix64(st);
-  return r;
-}
-
-// stream(base_seed, experiment, condition, trial) with the experiment already hashed
-__host__ __device__ __forceinline__ Xoshiro stream(uint64_t base_seed, uint64_t name_hash, uint64_t cond,
-                                                   uint64_t trial) {
-  uint64_t st = base_seed ^ name_hash;
-  uint64_t a = splitmix64(st);
-  st = a ^ cond;
-  uint64_t b = splitmix64(st);
-  st = b ^ trial;
-  return xoshiro_seed(splitmix64(st));
-}
-
-__host__ __device__ __forceinline__ void xoshiro_advance(Xoshiro& r) {
-  uint64_t t = r.s1 << 17;
-  r.s2 ^= r.s0;
-  r.s3 ^= r.s1;
-  r.s1 ^= r.s2;
-  r.s0 ^= r.s3;
-  r.s2 ^= t;
-  r.s3 = rotl64(r.s3, 45);
-}
-
-__host__ __device__ __forceinline__ uint64_t xoshiro_next(Xoshiro& r) {
-  uint64_t result = rotl64(r.s1 * 5, 7) * 9;
-  xoshiro_advance(r);
-  return result;
-}
+// Xoshiro, splitmix64, xoshiro_seed, stream and xoshiro_next are in xoshiro.h.
 
 // state after n steps, n given by its jump polynomial x^n mod P(x)
 __device__ __forceinline__ void xoshiro_jump(Xoshiro& r, const uint64_t* poly) {

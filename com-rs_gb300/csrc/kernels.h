@@ -206,6 +206,29 @@ struct SparseArgs {
 void* sparse_kernel_ptr(int precision, int rule, bool layered);
 cudaError_t launch_sparse(void* kernel, const void* args, int grid, int threads, size_t smem, cudaStream_t stream);
 
+// ---- systematic encoders of generic codes (sparse_encode.cu)
+struct SumsEncodeArgs {
+  const uint8_t* info;      // [n_frames][k]
+  uint8_t* coded;           // [n_frames][n]
+  int64_t n_frames;
+  int32_t k, n, rank, words;
+  const int32_t* info_pos;  // k
+  const int32_t* pivots;    // rank
+  const uint32_t* pmat;     // words x rank, word-major
+};
+struct AccumulateEncodeArgs {
+  const uint8_t* info;       // [n_frames][k]
+  uint8_t* coded;            // [n_frames][n]
+  int64_t n_frames;
+  int32_t k, n, m;
+  const int32_t* row_start;  // m + 1
+  const int32_t* vars;       // edges
+};
+size_t sums_encode_smem(int words);
+size_t accumulate_encode_smem(int k, int m);
+cudaError_t launch_sums_encode(const SumsEncodeArgs& a, cudaStream_t stream);
+cudaError_t launch_accumulate_encode(const AccumulateEncodeArgs& a, cudaStream_t stream);
+
 // ---- the NR code through the generic decoder (nr_generic.cu)
 template <typename T>
 struct NrEpilogueArgs {

@@ -34,4 +34,42 @@ struct SparseCode {
 bool build_sparse_code(int n, int m, const int32_t* row_start, const int32_t* vars, SparseCode& out,
                        std::string& err);
 
+// The systematic encoder of a code: the information positions and how the parity bits
+// follow from the information bits.
+enum EncoderKind { kEncoderNone = -1, kEncoderSums = 0, kEncoderAccumulate = 1 };
+
+struct SparseEncoder {
+  int kind = kEncoderNone;
+  int k = 0;
+  std::vector<int32_t> info;    // k increasing positions: information bit i sits at info[i]
+  std::vector<int32_t> pivots;  // sums: the parity position of every leading row of the reduced H
+  int words = 0;                // sums: 32-bit words of a packed information word
+  // sums, words x pivots, word-major: bit b of word (w, t) is set when parity bit t sums
+  // information bit 32 w + b
+  std::vector<uint32_t> pmat;
+};
+
+// LdpcCode::from_rows (crates/com-fec/src/ldpc.rs:216-231): the reduced row echelon
+// form of H with the pivots searched from the last column to the first
+// (crates/com-math/src/gf2.rs:121-150); the information bits are the columns without a
+// pivot, and the parity bit of every leading row is the sum of the information bits
+// that row keeps.  False for a code without information bits.
+bool reduce_sums(const SparseCode& code, SparseEncoder& out, std::string& err);
+
+// LdpcCode::accumulate (ldpc.rs:233-256): an irregular repeat-accumulate code, check r
+// holding information bits (below k = n - m) and the parity bits k + r and, for r > 0,
+// k + r - 1 only.  False, with the reference's message, for another structure.
+bool check_accumulate(const SparseCode& code, SparseEncoder& out, std::string& err);
+
+// LdpcCode::peg (ldpc.rs:289-313, :586-634): progressive edge growth of a code of n
+// variables and n - k checks, every variable of degree var_degree, the ties broken by
+// Rng::new(seed).below.  rows[c] lists the variables of check c in the order they were
+// linked.  False, with the reference's message, for invalid sizes.
+bool peg_rows(int n, int k, int var_degree, uint64_t seed, std::vector<std::vector<int32_t>>& rows,
+              std::string& err);
+
+// LdpcCode::girth (ldpc.rs:412-446): the length of the shortest cycle of the Tanner
+// graph by a breadth-first search from every variable; 0 without cycle.
+int girth(const SparseCode& code);
+
 }  // namespace cbh

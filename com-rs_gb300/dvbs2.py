@@ -5,7 +5,8 @@ Follows ``crates/com-systems/src/dvbs2/fec.rs``: the (k_bch, k_ldpc, t) of Table
 (``ldpc_rows``, fec.rs:213-235): information bit l of group j, with the group's
 addresses x, sits in the checks (x + l q) mod (n - k), q = (n - k) / 360; check r then
 closes on the parity bits k + r - 1 (r > 0) and k + r, the dual-diagonal accumulator.
-The decoder defaults to the sum-product rule, as ``Dvbs2Fec::new`` sets it (fec.rs:262-264).
+The code is the IRA code of ``LdpcCode::accumulate`` and its decoder defaults to the
+sum-product rule, as ``Dvbs2Fec::new`` sets them (fec.rs:262-264).
 
 Only the LDPC part is here (the outer BCH code is not on the GPU path).
 """
@@ -65,10 +66,12 @@ def ldpc_rows(frame, rate):
 
 
 def Dvbs2Ldpc(frame, rate, rule="sum_product", **decoder):
-    """The GPU decoder (an :class:`Ldpc`) of the LDPC code of a DVB-S2 FECFRAME."""
+    """The LDPC code of a DVB-S2 FECFRAME on the GPU (an :class:`Ldpc`), with the
+    accumulate encoder of ``LdpcCode::accumulate`` as ``Dvbs2Fec::new`` builds it
+    (fec.rs:262)."""
     from .ldpc import Ldpc
 
     n, k, rows = ldpc_rows(frame, rate)
-    code = Ldpc(n, rows, rule=rule, **decoder)
-    code.k = k
+    code = Ldpc.accumulate(n, rows, rule=rule, **decoder)
+    assert code.k == k
     return code

@@ -240,6 +240,39 @@ cb_status cb_ldpc_decode(cb_ldpc* code, const void* llr, int64_t n_frames, void*
 /* the same on device buffers, enqueued on `stream` (NULL: the code's own stream) */
 cb_status cb_ldpc_decode_device(cb_ldpc* code, const void* llr_dev, int64_t n_frames, void* post_dev,
                                 int32_t* iterations_dev, void* stream);
+/* LdpcCode::set_decoder (bindings/com-py/src/fec/ldpc_code.rs:74-86): new decoder
+ * settings, checked as cb_ldpc_create checks them; the device tables are rebuilt on the
+ * next decode when the rule or the schedule changes, so no decode of this code may be
+ * in flight on another stream */
+cb_status cb_ldpc_set_decoder(cb_ldpc* code, int32_t rule, double alpha, int32_t layered, int32_t max_iterations);
+/* LdpcCode::girth (ldpc.rs:412-446): the length of the shortest cycle of the Tanner
+ * graph (0 without cycle); host only */
+cb_status cb_ldpc_girth(const cb_ldpc* code, int32_t* girth);
+/* The systematic encoder (host only; the encode calls below then run on the GPU):
+ * CB_ENC_SUMS is that of LdpcCode::from_rows (ldpc.rs:216-231): H reduced with the
+ * pivots searched from the last column (crates/com-math/src/gf2.rs:121-150), the
+ * columns without a pivot the information positions, every pivot bit a sum of
+ * information bits; CB_ENC_ACCUMULATE that of LdpcCode::accumulate (ldpc.rs:233-256):
+ * the first n - m bits the information, parity bit n - m + r the running sum of checks
+ * 0..r, for dual-diagonal (IRA) checks only (CB_ERR_CONFIG with the reference's message
+ * otherwise).  Writes k and, when info_positions is not NULL, the k information
+ * positions (at most n entries). */
+#define CB_ENC_SUMS 0
+#define CB_ENC_ACCUMULATE 1
+cb_status cb_ldpc_set_encoder(cb_ldpc* code, int32_t kind, int32_t* k, int32_t* info_positions);
+/* LdpcCode::encode_block (ldpc.rs:753-791) of n_frames blocks: k information bits per
+ * frame (u8, bit 0 used) into n coded bits per frame (u8); host buffers.  Needs an
+ * encoder (cb_ldpc_set_encoder). */
+cb_status cb_ldpc_encode(cb_ldpc* code, const uint8_t* info, int64_t n_frames, uint8_t* coded);
+/* the same on device buffers, enqueued on `stream` (NULL: the code's own stream) */
+cb_status cb_ldpc_encode_device(cb_ldpc* code, const uint8_t* info_dev, int64_t n_frames, uint8_t* coded_dev,
+                                void* stream);
+/* LdpcCode::peg (ldpc.rs:289-313, :586-634): the rows of a code of n variables and
+ * n - k checks by progressive edge growth, every variable of degree var_degree, the
+ * ties broken by Rng::new(seed) (crates/com-core/src/rng.rs); host only.  Writes
+ * row_start[n - k + 1] and vars[n var_degree], each row's variables in the order they
+ * were linked (the reference's rows, hence its alist files). */
+cb_status cb_ldpc_peg(int32_t n, int32_t k, int32_t var_degree, uint64_t seed, int32_t* row_start, int32_t* vars);
 
 /* cb_decode_device for callers that cannot allocate device memory (a host framework
  * that owns all device memory through its own pool, or a real-time loop that forbids

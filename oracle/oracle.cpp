@@ -150,6 +150,7 @@ struct Code {
   // generic (alist) codes: Encoder::Sums
   std::vector<int> info;
   std::vector<std::pair<int, std::vector<int>>> sums;
+  bool accumulate = false;  // Encoder::Accumulate (IRA codes)
   // decoder settings (ldpc.rs:165-172)
   Rule rule = RULE_SUM_PRODUCT;
   double alpha = 0.8;
@@ -677,6 +678,34 @@ static bool from_rows(Code& c) {
   return true;
 }
 
+// LdpcCode::accumulate (ldpc.rs:241-256): the dual-diagonal structure is checked by the
+// library under test; the oracle only takes k = n - m and the information bits first
+static bool from_rows_accumulate(Code& c) {
+  int m = (int)c.rows.size();
+  if (!(m > 0 && m < c.n)) { c.error = "bad accumulate code size"; return false; }
+  c.k = c.n - m;
+  c.info.clear();
+  for (int i = 0; i < c.k; i++) c.info.push_back(i);
+  c.accumulate = true;
+  c.core = 0;
+  assemble_start(c);
+  return true;
+}
+
+// Encoder::Accumulate (ldpc.rs:765-772): parity bit k + r is the running sum of the
+// information bits of checks 0..r
+static void encode_accumulate(const Code& c, const uint8_t* u, uint8_t* cw) {
+  std::fill(cw, cw + c.n, 0);
+  for (int i = 0; i < c.k; i++) cw[i] = u[i] & 1;
+  uint8_t prev = 0;
+  for (size_t r = 0; r < c.rows.size(); r++) {
+    uint8_t a = 0;
+    for (int v : c.rows[r]) if (v < c.k) a ^= cw[v];
+    prev ^= a;
+    cw[c.k + r] = prev;
+  }
+}
+
 static void encode_sums(const Code& c, const uint8_t* u, uint8_t* cw) {
   std::fill(cw, cw + c.n, 0);
   for (size_t i = 0; i < c.info.size(); i++) cw[c.info[i]] = u[i] & 1;
@@ -861,6 +890,29 @@ void* or_code_from_alist(const char* text, char* err, int errlen) {
   return c;
 }
 
+// a generic code from its rows (row_start[m + 1], vars): Encoder::Sums of from_rows, or
+// Encoder::Accumulate when `accumulate` is set
+void* or_code_from_rows(int n, int m, const int32_t* row_start, const int32_t* vars, int accumulate, char* err,
+                        int errlen) {
+  Code* c = new Code();
+  c->n = n;
+  c->rows.assign(m, {});
+  for (int r = 0; r < m; r++)
+    for (int e = row_start[r]; e < row_start[r + 1]; e++) c->rows[r].push_back(vars[e]);
+  if (!(accumulate ? from_rows_accumulate(*c) : from_rows(*c))) {
+    if (err && errlen > 0) snprintf(err, errlen, "%s", c->error.c_str());
+    delete c;
+    return nullptr;
+  }
+  return c;
+}
+
+// the information positions of a generic code (k entries)
+void or_code_info_positions(void* h, int32_t* out) {
+  Code* c = (Code*)h;
+  for (size_t i = 0; i < c->info.size(); i++) out[i] = c->info[i];
+}
+
 void or_code_free(void* h) { delete (Code*)h; }
 
 // out[0..8] = bg, z, k_info, e, K, n_full, rows, edges, ils
@@ -904,6 +956,7 @@ void or_encode(void* h, const uint8_t* info, uint8_t* out) {
 void or_encode_full(void* h, const uint8_t* u, uint8_t* out) {
   Code* c = (Code*)h;
   if (c->core) encode_core(*c, u, out);
+  else if (c->accumulate) encode_accumulate(*c, u, out);
   else encode_sums(*c, u, out);
 }
 

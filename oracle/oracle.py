@@ -45,6 +45,9 @@ def lib():
         L.or_code_new.argtypes = [i32, i32, i32, i32, i32, i32, C.c_char_p, i32]
         L.or_code_from_alist.restype = vp
         L.or_code_from_alist.argtypes = [C.c_char_p, C.c_char_p, i32]
+        L.or_code_from_rows.restype = vp
+        L.or_code_from_rows.argtypes = [i32, i32, vp, vp, i32, C.c_char_p, i32]
+        L.or_code_info_positions.argtypes = [vp, vp]
         L.or_code_free.argtypes = [vp]
         L.or_code_info.argtypes = [vp, vp]
         L.or_code_bit_map.argtypes = [vp, vp]
@@ -129,11 +132,18 @@ def demap_exact(m, y, sigma2):
 
 
 class Code:
-    """The oracle's NrLdpc (or a generic LdpcCode read from an alist text)."""
+    """The oracle's NrLdpc, or a generic LdpcCode read from an alist text or given by its
+    rows (the encoder of from_rows, or of accumulate)."""
 
-    def __init__(self, k_info=None, e=None, bg=0, z=0, rv=0, qm=1, alist=None):
+    def __init__(self, k_info=None, e=None, bg=0, z=0, rv=0, qm=1, alist=None, rows=None, n=None,
+                 accumulate=False):
         err = C.create_string_buffer(256)
-        if alist is not None:
+        if rows is not None:
+            start = np.zeros(len(rows) + 1, np.int32)
+            start[1:] = np.cumsum([len(r) for r in rows])
+            flat = np.array([v for r in rows for v in r], np.int32)
+            self.h = lib().or_code_from_rows(n, len(rows), _p(start), _p(flat), int(bool(accumulate)), err, 256)
+        elif alist is not None:
             self.h = lib().or_code_from_alist(alist.encode(), err, 256)
         else:
             self.h = lib().or_code_new(k_info, e, bg, z, rv, qm, err, 256)
@@ -171,6 +181,11 @@ class Code:
         info = np.ascontiguousarray(info, np.uint8)
         out = np.zeros(self.e, np.uint8)
         lib().or_encode(self.h, _p(info), _p(out))
+        return out
+
+    def info_positions(self):
+        out = np.zeros(self.k, np.int32)
+        lib().or_code_info_positions(self.h, _p(out))
         return out
 
     def encode_full(self, u):

@@ -9,7 +9,9 @@ against AFF3CT's recorded curves.
 * the four LDPC fixtures of validation/tests/aff3ct.rs:219-230 (PEG(576, 288) and
   PEG(648, 540); BPSK, sigma^2 = 1 / (2 R Eb/N0)): frame error rates whose 99 % Wilson
   intervals overlap AFF3CT's;
-* the generic decoder on the lifted rows of an NR code equals the NR decoder.
+* the generic decoder on the lifted rows of an NR code equals the NR decoder;
+* the encoders (from_rows' GF(2) sums, accumulate) equal the oracle's codewords, and
+  set_decoder gives the decoder a fresh code with the same settings has.
 """
 
 import json
@@ -211,3 +213,96 @@ def test_dvbs2_normal_frame_decodes_with_posteriors_in_global_memory(cb, rule):
     assert (post > 0).all() and (its < 30).all() and (its > 1).all()
     post2, its2 = code.decode_llr(llr)
     assert np.array_equal(post.view(np.uint64), post2.view(np.uint64)) and np.array_equal(its, its2)
+
+
+# ---------------------------------------------------------------- encoders
+
+def _encoder_case(cb, kind):
+    """(GPU code, oracle rows, n, accumulate) of a named case."""
+    from test_sparse_host import HAMMING
+
+    if kind.startswith("peg"):
+        n, k = {"peg576": (576, 288), "peg648": (648, 540)}[kind]
+        return n, cb.ldpc.peg_rows(n, k), False
+    if kind == "hamming":
+        n, rows = cb.parse_alist(HAMMING)
+        return n, rows, False
+    if kind == "rank_deficient":
+        rng = np.random.default_rng(4)
+        rows = [sorted(rng.choice(120, size=7, replace=False).tolist()) for _ in range(50)]
+        return 120, rows + rows[:6] + [sorted(set(rows[0]) ^ set(rows[1]))], False
+    frame, rate = {"dvbs2_short_1_2": ("short", "1/2"), "dvbs2_normal_1_4": ("normal", "1/4")}[kind]
+    n, _, rows = cb.dvbs2.ldpc_rows(frame, rate)
+    return n, rows, True
+
+
+@pytest.mark.parametrize("kind, frames", [("peg576", 5000), ("peg648", 300), ("hamming", 64),
+                                          ("rank_deficient", 200), ("dvbs2_short_1_2", 96),
+                                          ("dvbs2_normal_1_4", 24)])
+def test_encode_equals_the_oracle(cb, O, kind, frames):
+    # LdpcCode::encode_block (ldpc.rs:753-791): Encoder::Sums of from_rows, or
+    # Encoder::Accumulate of the DVB-S2 codes; 5000 frames run the grid-stride loop
+    n, rows, acc = _encoder_case(cb, kind)
+    code = cb.Ldpc.accumulate(n, rows) if acc else cb.Ldpc(n, rows)
+    ref = O.Code(rows=rows, n=n, accumulate=acc)
+    assert code.k == ref.k
+    rng = np.random.default_rng(len(kind) * 1000 + frames)
+    u = rng.integers(0, 2, (frames, code.k), dtype=np.uint8)
+    # only bit 0 of every byte counts (c[p] = b & 1)
+    noisy = u | (rng.integers(0, 128, u.shape, dtype=np.uint8) << 1).astype(np.uint8)
+    c = code.encode(noisy)
+    check = range(frames) if frames <= 300 else rng.choice(frames, 300, replace=False)
+    for f in check:
+        want = ref.encode_full(u[f])
+        assert np.array_equal(c[f], want), f
+        assert ref.is_codeword(c[f]), f
+    assert np.array_equal(c[:, code.info_positions()], u)
+    assert np.array_equal(code.encode(u.reshape(-1)), c.reshape(-1))
+    assert code.encode(np.zeros((0, code.k), np.uint8)).shape == (0, n)
+
+
+def test_encode_on_device_buffers(cb):
+    import ctypes as C
+
+    torch = pytest.importorskip("torch")
+    code = cb.Ldpc.peg(576, 288)
+    rng = np.random.default_rng(8)
+    u = rng.integers(0, 2, (700, 288), dtype=np.uint8)
+    want = code.encode(u)
+    u_d = torch.from_numpy(u).cuda()
+    c_d = torch.full((700, 576), 7, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    st = cb.lib().cb_ldpc_encode_device(code._h, C.c_void_p(u_d.data_ptr()), 700, C.c_void_p(c_d.data_ptr()),
+                                        C.c_void_p(s.cuda_stream))
+    assert st == 0
+    s.synchronize()
+    assert np.array_equal(c_d.cpu().numpy(), want)
+
+
+def test_encode_decode_round_trip(cb):
+    # bindings/com-py/src/fec/ldpc_code.rs:150-156: decode(2 - 4 encode(b)) == b with the
+    # default decoder (layered sum-product, 50 iterations)
+    code = cb.Ldpc.peg(96, 48)
+    b = np.random.default_rng(1).integers(0, 2, 48 * 10, dtype=np.uint8)
+    c = code.encode(b)
+    assert c.size == 960
+    assert np.array_equal(code.decode(2.0 - 4.0 * c), b)
+    assert np.array_equal(code.decode((2.0 - 4.0 * c).reshape(10, 96)), b.reshape(10, 48))
+
+
+def test_set_decoder_equals_a_fresh_code(cb, O):
+    # a code whose decoder is changed decodes as a code built with the new settings
+    text = open(os.path.join(GOLDEN, "peg_n576_k288.alist")).read()
+    n, rows = cb.parse_alist(text)
+    ref = O.Code(alist=text)
+    _, llr = _frames(O, ref, 2.0, 0, 128)
+    code = cb.Ldpc(n, rows, rule="normalized_min_sum", alpha=0.75, max_iterations=20)
+    code.decode_llr(llr)
+    for rule, alpha, layered, iters in (("offset_min_sum", 0.15, False, 20), ("normalized_min_sum", 0.8, True, 7),
+                                        ("sum_product", 0.0, True, 30), ("min_sum", 0.3, False, 12)):
+        code.set_decoder(rule, alpha=alpha, layered=layered, max_iterations=iters)
+        post, its = code.decode_llr(llr)
+        fresh = cb.Ldpc(n, rows, rule=rule, alpha=alpha, layered=layered, max_iterations=iters)
+        post_f, its_f = fresh.decode_llr(llr)
+        assert np.array_equal(post.view(np.uint64), post_f.view(np.uint64)), rule
+        assert np.array_equal(its, its_f), rule
