@@ -11,7 +11,10 @@ the reference's Python surface for this path:
 * :class:`Ldpc` -- the reference's generic ``LdpcCode`` decoder (any parity-check matrix,
   alist files, sum-product or min-sum, layered or flooding; crates/com-fec/src/ldpc.rs);
 * :func:`run` -- a campaign over an Eb/N0 grid with the ``min_errors(...).or(max_trials)``
-  stopping rule of com-sim (crates/com-sim/src/stopping.rs:64-265).
+  stopping rule of com-sim (crates/com-sim/src/stopping.rs:64-265);
+* :class:`Link` and :func:`run_spec` -- the link ``fec_encode -> map -> awgn_ebn0 ->
+  demap -> fec_decode`` of a com-spec specification over a PEG code (specs/bicm_ldpc.yaml)
+  and the campaign of such a specification.
 
 The compute runs only in the CUDA library: there is no CPU fallback.  Importing works
 without a GPU; creating a code object needs one.
@@ -26,6 +29,7 @@ from .campaign import Grid, Stop, run  # noqa: F401
 from .dvbs2 import Dvbs2Ldpc  # noqa: F401
 from .ldpc import Ldpc, parse_alist  # noqa: F401
 from .mix import MIX_ITEM_DTYPE, MixBatch, autotune, draw_mixed_batch  # noqa: F401
+from .spec import LINK_DTYPE, Link, load_yaml, run_spec  # noqa: F401
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcomrs_gb300.so")
@@ -102,6 +106,13 @@ SYMBOLS = [
     ("cb_ldpc_encode", _i32, [_vp, _vp, _i64, _vp]),
     ("cb_ldpc_encode_device", _i32, [_vp, _vp, _i64, _vp, _vp]),
     ("cb_ldpc_peg", _i32, [_i32, _i32, _i32, _u64, _vp, _vp]),
+    ("cb_link_create", _i32, [_vp, _i32, _i32, _i32, _u64, _i32, C.POINTER(_vp)]),
+    ("cb_link_destroy", None, [_vp]),
+    ("cb_link_last_error", C.c_char_p, [_vp]),
+    ("cb_link_info", _i32, [_vp, _vp]),
+    ("cb_link_interleaver", _i32, [_vp, _vp]),
+    ("cb_link_run_trials", _i32, [_vp, _u64, _u64, _u64, _u64, _i64, _dbl, _vp]),
+    ("cb_link_generate", _i32, [_vp, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp, _vp]),
 ]
 
 _lib = None

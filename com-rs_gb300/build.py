@@ -22,7 +22,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-f
               "--expt-relaxed-constexpr"] + ARCH
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
-CU = ["decode.cu", "gen.cu", "nms_learned.cu", "mix.cu", "sparse.cu", "sparse_encode.cu", "nr_generic.cu", "capi.cu",
+CU = ["decode.cu", "gen.cu", "nms_learned.cu", "mix.cu", "sparse.cu", "sparse_encode.cu", "link.cu", "nr_generic.cu", "capi.cu",
       "capi_mix.cu", "capi_sparse.cu"]
 CPP = ["code_host.cpp", "sparse_host.cpp"]
 

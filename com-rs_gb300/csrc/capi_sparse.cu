@@ -56,12 +56,12 @@ struct cb_ldpc {
   size_t info_cap = 0;
   void* d_coded = nullptr;
   size_t coded_cap = 0;
-  std::string err;
+  mutable std::string err;  // the last error, set by const calls too
 };
 
 namespace {
 
-cb_status lfail(cb_ldpc* c, cb_status s, const std::string& msg) {
+cb_status lfail(const cb_ldpc* c, cb_status s, const std::string& msg) {
   if (c) c->err = msg;
   g_ldpc_thread_error = msg;
   return s;
@@ -287,6 +287,165 @@ cb_status check_decoder_settings(int32_t rule, double alpha, int32_t max_iterati
 
 }  // namespace
 
+// ------------------------------------------------------------------ the spec link
+struct cb_link {
+  std::mutex mu;
+  cb_ldpc* code = nullptr;
+  int blocks = 1, m = 0, mbits = 0, n_pad = 0, bpc = 0, spc = 0, exact = 0;
+  bool interleave = false;
+  uint64_t il_seed = 0;
+  double log_m = 0;
+  std::vector<double> pts;
+  std::vector<uint64_t> jumps;
+  std::vector<int32_t> perm, lookup;
+  int side = 0;
+  double step = 0, re0 = 0, im0 = 0;
+  bool dev_ready = false;
+  int32_t* d_tab = nullptr;   // perm (n x blocks, when interleaved) then lookup (m)
+  double* d_points = nullptr;
+  uint64_t* d_jumps = nullptr;
+  void* d_llr = nullptr;
+  size_t llr_cap = 0;
+  void* d_post = nullptr;
+  size_t post_cap = 0;
+  void* d_iters = nullptr;
+  size_t iters_cap = 0;
+  void* d_payload = nullptr;
+  size_t payload_cap = 0;
+  void* d_raw = nullptr;
+  size_t raw_cap = 0;
+  void* d_rec = nullptr;
+  size_t rec_cap = 0;
+  mutable std::string err;  // the last error, set by const calls too
+};
+
+namespace {
+
+thread_local std::string g_link_thread_error;
+
+cb_status kfail(const cb_link* l, cb_status s, const std::string& msg) {
+  if (l) l->err = msg;
+  g_link_thread_error = msg;
+  return s;
+}
+
+#define LINK_CUDA(l, call)                                                                      \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) return kfail((l), CB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// the axis levels of nearest.rs Slicer::detect: sorted, equal within 1e-9 of the span
+// merged
+std::vector<double> axis_levels(std::vector<double> l) {
+  std::sort(l.begin(), l.end());
+  const double span = std::max(std::fabs(l.back() - l[0]), 1e-300);
+  std::vector<double> out;
+  for (double v : l)
+    if (out.empty() || std::fabs(out.back() - v) > 1e-9 * span) out.push_back(v);
+  return out;
+}
+
+size_t link_trial_bytes(const cb_link* l) {
+  const size_t nb = (size_t)l->code->host.n * l->blocks;
+  return nb * 16 + (size_t)l->blocks * 4 + (size_t)l->blocks * ((l->code->enc.k + 31) / 32) * 4 + 4 +
+         sizeof(cbk::LinkRecord);
+}
+
+cb_status link_ensure_device(cb_link* l) {
+  if (l->dev_ready) return CB_OK;
+  cb_ldpc* c = l->code;
+  if (cb_status st = ensure_encoder(c)) return kfail(l, st, c->err);
+  if (cb_status st = ensure_device(c)) return kfail(l, st, c->err);
+  std::vector<int32_t> tab = l->perm;
+  tab.insert(tab.end(), l->lookup.begin(), l->lookup.end());
+  LINK_CUDA(l, cudaMalloc(&l->d_tab, tab.size() * 4));
+  LINK_CUDA(l, cudaMemcpy(l->d_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
+  LINK_CUDA(l, cudaMalloc(&l->d_points, l->pts.size() * 8));
+  LINK_CUDA(l, cudaMemcpy(l->d_points, l->pts.data(), l->pts.size() * 8, cudaMemcpyHostToDevice));
+  LINK_CUDA(l, cudaMalloc(&l->d_jumps, l->jumps.size() * 8));
+  LINK_CUDA(l, cudaMemcpy(l->d_jumps, l->jumps.data(), l->jumps.size() * 8, cudaMemcpyHostToDevice));
+  const size_t smem = cbk::link_gen_smem_bytes(l->m, l->mbits, c->enc.k, c->host.n, l->blocks, l->n_pad);
+  if (smem > kEncodeSmemLimit) return kfail(l, CB_ERR_CONFIG, "the trial does not fit the generator's shared memory");
+  l->dev_ready = true;
+  return CB_OK;
+}
+
+// trials [first, first + n) into the link's device buffers: generation, decoding and,
+// when `count` is set, the records
+cb_status link_run_device(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first, int64_t n,
+                          double ebn0_db, bool count) {
+  cb_ldpc* c = l->code;
+  const cbh::SparseEncoder& e = c->enc;
+  const int nb = c->host.n * l->blocks, wk = (e.k + 31) / 32;
+  LINK_CUDA(l, grow_buf(&l->d_llr, l->llr_cap, (size_t)n * nb * 8));
+  LINK_CUDA(l, grow_buf(&l->d_post, l->post_cap, (size_t)n * nb * 8));
+  LINK_CUDA(l, grow_buf(&l->d_iters, l->iters_cap, (size_t)n * l->blocks * 4));
+  LINK_CUDA(l, grow_buf(&l->d_payload, l->payload_cap, (size_t)n * l->blocks * wk * 4));
+  LINK_CUDA(l, grow_buf(&l->d_raw, l->raw_cap, (size_t)n * 4));
+  LINK_CUDA(l, grow_buf(&l->d_rec, l->rec_cap, (size_t)n * sizeof(cbk::LinkRecord)));
+  cbk::LinkGenArgs a;
+  a.k = e.k;
+  a.n = c->host.n;
+  a.blocks = l->blocks;
+  a.rank = (int32_t)e.pivots.size();
+  a.info_pos = c->d_enc;
+  a.pivots = c->d_enc + e.k;
+  a.pmat = reinterpret_cast<const uint32_t*>(c->d_enc + e.k + e.pivots.size());
+  a.perm = l->interleave ? l->d_tab : nullptr;
+  a.m = l->m;
+  a.mbits = l->mbits;
+  a.n_pad = l->n_pad;
+  a.bits_per_chunk = l->bpc;
+  a.syms_per_chunk = l->spc;
+  a.points = l->d_points;
+  a.log_m = l->log_m;
+  // b = log2 M k / n (com-spec blocks/channel.rs:145-149, block.rs:59-61), times db2lin
+  const double rate = (double)e.k / (double)c->host.n;
+  a.b_ebn0 = ((double)l->mbits * rate) * std::pow(10.0, ebn0_db / 10.0);
+  a.exact = l->exact;
+  a.jumps = l->d_jumps;
+  a.side = l->side;
+  a.step = l->step;
+  a.re0 = l->re0;
+  a.im0 = l->im0;
+  a.lookup = l->d_tab + l->perm.size();
+  a.seed = seed;
+  a.name_hash = name_hash;
+  a.cond = cond;
+  a.first_trial = first;
+  a.n_trials = n;
+  a.llr_out = (double*)l->d_llr;
+  a.payload_out = (uint32_t*)l->d_payload;
+  a.raw_errors_out = (uint32_t*)l->d_raw;
+  LINK_CUDA(l, cbk::launch_link_gen(a, c->stream));
+  if (cb_status st = decode_impl<double>(c, (const double*)l->d_llr, n * l->blocks, (double*)l->d_post,
+                                         (int32_t*)l->d_iters, c->stream))
+    return kfail(l, st, c->err);
+  if (count) {
+    cbk::LinkCountArgs ca;
+    ca.k = e.k;
+    ca.n = c->host.n;
+    ca.blocks = l->blocks;
+    ca.info_pos = c->d_enc;
+    ca.post = (const double*)l->d_post;
+    ca.iters = (const int32_t*)l->d_iters;
+    ca.payload = (const uint32_t*)l->d_payload;
+    ca.raw_errors = (const uint32_t*)l->d_raw;
+    ca.n_trials = n;
+    ca.out = (cbk::LinkRecord*)l->d_rec;
+    LINK_CUDA(l, cbk::launch_link_count(ca, c->stream));
+  }
+  return CB_OK;
+}
+
+// trials per chunk: at most 1 GB of buffers
+int64_t link_chunk(const cb_link* l, int64_t n) {
+  return std::max<int64_t>(1, std::min<int64_t>(n, (int64_t)(((size_t)1 << 30) / link_trial_bytes(l))));
+}
+
+}  // namespace
+
 extern "C" {
 
 cb_status cb_ldpc_create(int32_t n, int32_t m, const int32_t* row_start, const int32_t* vars, int32_t rule,
@@ -334,7 +493,7 @@ void cb_ldpc_destroy(cb_ldpc* c) {
 const char* cb_ldpc_last_error(const cb_ldpc* c) { return c ? c->err.c_str() : g_ldpc_thread_error.c_str(); }
 
 cb_status cb_ldpc_info(const cb_ldpc* c, int64_t* info) {
-  if (!c || !info) return lfail(nullptr, CB_ERR_CONFIG, "null argument");
+  if (!c || !info) return lfail(c, CB_ERR_CONFIG, "null argument");
   const cbh::SparseCode& h = c->host;
   const int64_t v[8] = {h.n, h.m, h.edges, h.max_row_degree, h.max_col_degree, h.levels, h.max_level_rows,
                         c->layered};
@@ -410,7 +569,7 @@ cb_status cb_ldpc_set_decoder(cb_ldpc* c, int32_t rule, double alpha, int32_t la
 }
 
 cb_status cb_ldpc_girth(const cb_ldpc* c, int32_t* girth) {
-  if (!c || !girth) return lfail(nullptr, CB_ERR_CONFIG, "null argument");
+  if (!c || !girth) return lfail(c, CB_ERR_CONFIG, "null argument");
   *girth = cbh::girth(c->host);
   return CB_OK;
 }
@@ -480,6 +639,151 @@ cb_status cb_ldpc_peg(int32_t n, int32_t k, int32_t var_degree, uint64_t seed, i
   for (size_t r = 0; r < rows.size(); r++) {
     for (int32_t v : rows[r]) vars[e++] = v;
     row_start[r + 1] = e;
+  }
+  return CB_OK;
+}
+
+
+cb_status cb_link_create(cb_ldpc* code, int32_t blocks, int32_t modulation_order, int32_t interleave,
+                         uint64_t interleaver_seed, int32_t exact_demap, cb_link** out) {
+  if (!out) return kfail(nullptr, CB_ERR_CONFIG, "null output pointer");
+  *out = nullptr;
+  if (!code) return kfail(nullptr, CB_ERR_CONFIG, "null code");
+  if (code->precision != CB_F64) return kfail(nullptr, CB_ERR_CONFIG, "the link runs in f64: create the code with CB_F64");
+  if (code->enc.kind != cbh::kEncoderSums)
+    return kfail(nullptr, CB_ERR_CONFIG, "the link needs the from_rows encoder: cb_ldpc_set_encoder(CB_ENC_SUMS)");
+  if (blocks < 1) return kfail(nullptr, CB_ERR_CONFIG, "blocks must be >= 1");
+  const int64_t nb = (int64_t)code->host.n * blocks;
+  if (nb > ((int64_t)1 << 24)) return kfail(nullptr, CB_ERR_CONFIG, "n x blocks must be at most 2^24");
+  cb_link* l = new cb_link;
+  l->code = code;
+  l->blocks = blocks;
+  l->m = modulation_order;
+  if (!cbh::qam_points(modulation_order, l->pts, l->log_m)) {
+    delete l;
+    return kfail(nullptr, CB_ERR_CONFIG, "modulation order must be 4, 16, 64 or 256");
+  }
+  const cbh::GenTables t = cbh::gen_tables(code->enc.k * blocks, (int)nb, modulation_order, cbk::kGenThreads);
+  l->mbits = t.mbits;
+  l->n_pad = t.n_pad;
+  l->bpc = t.bits_per_chunk;
+  l->spc = t.syms_per_chunk;
+  l->jumps = t.jumps;
+  l->exact = exact_demap ? 1 : 0;
+  l->interleave = interleave != 0;
+  l->il_seed = interleaver_seed;
+  if (l->interleave) {
+    // Interleaver::random (interleaving.rs:63-67): Rng::new(seed).shuffle (rng.rs:218-222)
+    l->perm.resize(nb);
+    for (int64_t i = 0; i < nb; i++) l->perm[i] = (int32_t)i;
+    cbd::Xoshiro r = cbd::xoshiro_seed(interleaver_seed);
+    for (int64_t i = nb - 1; i >= 1; i--) std::swap(l->perm[i], l->perm[cbd::xoshiro_below(r, (uint64_t)i + 1)]);
+  }
+  // the grid slicer of the square QAM (nearest.rs Slicer::detect)
+  std::vector<double> re(l->m), im(l->m);
+  for (int i = 0; i < l->m; i++) {
+    re[i] = l->pts[2 * i];
+    im[i] = l->pts[2 * i + 1];
+  }
+  const std::vector<double> lre = axis_levels(re), lim = axis_levels(im);
+  l->side = (int)lre.size();
+  l->step = (lre.back() - lre[0]) / (double)(l->side - 1);
+  l->re0 = lre[0];
+  l->im0 = lim[0];
+  l->lookup.assign(l->m, 0);
+  for (int i = 0; i < l->m; i++) {
+    const int col = (int)std::round((re[i] - lre[0]) / l->step), row = (int)std::round((im[i] - lim[0]) / l->step);
+    l->lookup[row * l->side + col] = i;
+  }
+  *out = l;
+  return CB_OK;
+}
+
+void cb_link_destroy(cb_link* l) {
+  if (!l) return;
+  if (l->dev_ready || l->d_llr) {
+    cudaSetDevice(l->code->device);
+    if (l->code->stream) cudaStreamSynchronize(l->code->stream);
+    cudaFree(l->d_tab);
+    cudaFree(l->d_points);
+    cudaFree(l->d_jumps);
+    cudaFree(l->d_llr);
+    cudaFree(l->d_post);
+    cudaFree(l->d_iters);
+    cudaFree(l->d_payload);
+    cudaFree(l->d_raw);
+    cudaFree(l->d_rec);
+  }
+  delete l;
+}
+
+const char* cb_link_last_error(const cb_link* l) { return l ? l->err.c_str() : g_link_thread_error.c_str(); }
+
+cb_status cb_link_info(const cb_link* l, int64_t info[8]) {
+  if (!l || !info) return kfail(l, CB_ERR_CONFIG, "null argument");
+  const int64_t nb = (int64_t)l->code->host.n * l->blocks;
+  const int64_t v[8] = {l->code->enc.k, l->code->host.n, l->blocks, l->m, nb + l->n_pad,
+                        (int64_t)l->code->enc.k * l->blocks, l->n_pad, l->interleave ? 1 : 0};
+  std::copy(v, v + 8, info);
+  return CB_OK;
+}
+
+cb_status cb_link_interleaver(const cb_link* l, int32_t* perm) {
+  if (!l || !perm) return kfail(l, CB_ERR_CONFIG, "null argument");
+  if (!l->interleave) return kfail(l, CB_ERR_CONFIG, "the link has no interleaver");
+  std::copy(l->perm.begin(), l->perm.end(), perm);
+  return CB_OK;
+}
+
+cb_status cb_link_run_trials(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_t condition, uint64_t first_trial,
+                             int64_t n_trials, double ebn0_db, cb_link_record* out) {
+  if (!l) return kfail(nullptr, CB_ERR_CONFIG, "null link");
+  if (n_trials < 0) return kfail(l, CB_ERR_SHAPE, "n_trials must be >= 0");
+  if (n_trials == 0) return CB_OK;
+  if (!out) return kfail(l, CB_ERR_SHAPE, "null records");
+  std::lock_guard<std::mutex> lock(l->mu);
+  std::lock_guard<std::mutex> lock_code(l->code->mu);
+  if (cb_status st = link_ensure_device(l)) return st;
+  const int64_t chunk = link_chunk(l, n_trials);
+  for (int64_t f0 = 0; f0 < n_trials; f0 += chunk) {
+    const int64_t cnt = std::min(chunk, n_trials - f0);
+    if (cb_status st = link_run_device(l, seed, name_hash, condition, first_trial + f0, cnt, ebn0_db, true)) return st;
+    LINK_CUDA(l, cudaMemcpyAsync(out + f0, l->d_rec, cnt * sizeof(cb_link_record), cudaMemcpyDeviceToHost,
+                                 l->code->stream));
+    LINK_CUDA(l, cudaStreamSynchronize(l->code->stream));
+  }
+  return CB_OK;
+}
+
+cb_status cb_link_generate(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_t condition, uint64_t first_trial,
+                           int64_t n_trials, double ebn0_db, double* llr, uint8_t* payload, uint32_t* raw_errors) {
+  if (!l) return kfail(nullptr, CB_ERR_CONFIG, "null link");
+  if (n_trials < 0) return kfail(l, CB_ERR_SHAPE, "n_trials must be >= 0");
+  if (n_trials == 0) return CB_OK;
+  std::lock_guard<std::mutex> lock(l->mu);
+  std::lock_guard<std::mutex> lock_code(l->code->mu);
+  if (cb_status st = link_ensure_device(l)) return st;
+  const int k = l->code->enc.k, nb = l->code->host.n * l->blocks, wk = (k + 31) / 32;
+  const int64_t chunk = link_chunk(l, n_trials);
+  std::vector<uint32_t> words;
+  for (int64_t f0 = 0; f0 < n_trials; f0 += chunk) {
+    const int64_t cnt = std::min(chunk, n_trials - f0);
+    if (cb_status st = link_run_device(l, seed, name_hash, condition, first_trial + f0, cnt, ebn0_db, false))
+      return st;
+    cudaStream_t s = l->code->stream;
+    if (llr) LINK_CUDA(l, cudaMemcpyAsync(llr + f0 * nb, l->d_llr, cnt * nb * 8, cudaMemcpyDeviceToHost, s));
+    if (raw_errors) LINK_CUDA(l, cudaMemcpyAsync(raw_errors + f0, l->d_raw, cnt * 4, cudaMemcpyDeviceToHost, s));
+    if (payload) {
+      words.resize((size_t)cnt * l->blocks * wk);
+      LINK_CUDA(l, cudaMemcpyAsync(words.data(), l->d_payload, words.size() * 4, cudaMemcpyDeviceToHost, s));
+    }
+    LINK_CUDA(l, cudaStreamSynchronize(s));
+    if (payload)
+      for (int64_t t = 0; t < cnt; t++)
+        for (int b = 0; b < l->blocks; b++)
+          for (int i = 0; i < k; i++)
+            payload[((f0 + t) * l->blocks + b) * k + i] =
+                (uint8_t)((words[((size_t)t * l->blocks + b) * wk + i / 32] >> (i % 32)) & 1u);
   }
   return CB_OK;
 }

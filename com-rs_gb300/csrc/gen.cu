@@ -35,6 +35,7 @@
 #include "crmath.cuh"
 #include "decode_common.cuh"
 #include "kernels.h"
+#include "qam_f64.cuh"
 
 namespace cbk {
 namespace {
@@ -283,46 +284,15 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
   T* out = a.llr_out;
   if (sizeof(T) == 8) {
     const double sd = __dsqrt_rn(sigma2);
-    const double uniform = -a.log_m;
     for (int s = s0; s < s1; s++) {
-      double u1 = (double)(cbd::xoshiro_next(r) >> 11) * (1.0 / 9007199254740992.0);
-      double u2 = (double)(cbd::xoshiro_next(r) >> 11) * (1.0 / 9007199254740992.0);
-      double l = crm::cr_log(__dsub_rn(1.0, u1));
-      double rad = __dmul_rn(__dsqrt_rn(__dmul_rn(-2.0, l)), 0.70710678118654752440);
-      double sn, cs;
-      crm::cr_sincos(__dmul_rn(6.283185307179586, u2), &sn, &cs);
-      double nre = __dmul_rn(rad, cs), nim = __dmul_rn(rad, sn);
-      int li = lab[s];
-      double yre = __dadd_rn(pts[2 * li], __dmul_rn(nre, sd));
-      double yim = __dadd_rn(pts[2 * li + 1], __dmul_rn(nim, sd));
-      for (int o = 0; o < a.mbits; o++) {
-        int t = s * a.mbits + o;
-        if (t >= c.e) break;
-        int shift = a.mbits - 1 - o;
-        double m0 = -INFINITY, m1 = -INFINITY;
-        for (int i = 0; i < a.m; i++) {
-          double dr = __dsub_rn(yre, pts[2 * i]), di = __dsub_rn(yim, pts[2 * i + 1]);
-          double ns = __dadd_rn(__dmul_rn(dr, dr), __dmul_rn(di, di));
-          double met = __dadd_rn(__ddiv_rn(-ns, sigma2), uniform);
-          if ((i >> shift) & 1) m1 = fmax(m1, met);
-          else m0 = fmax(m0, met);
-        }
-        if (a.exact && isfinite(m0) && isfinite(m1)) {
-          // LabelHalves (demapper.rs:82-133): sums of exp(metric - max) in label order,
-          // L = m0 + ln s0 - m1 - ln s1; CUDA's exp and log where the reference calls libm
-          double s0 = 0.0, s1 = 0.0;
-          for (int i = 0; i < a.m; i++) {
-            double dr = __dsub_rn(yre, pts[2 * i]), di = __dsub_rn(yim, pts[2 * i + 1]);
-            double ns = __dadd_rn(__dmul_rn(dr, dr), __dmul_rn(di, di));
-            double met = __dadd_rn(__ddiv_rn(-ns, sigma2), uniform);
-            if ((i >> shift) & 1) s1 = __dadd_rn(s1, exp(__dsub_rn(met, m1)));
-            else s0 = __dadd_rn(s0, exp(__dsub_rn(met, m0)));
-          }
-          out[t] = (T)__dsub_rn(__dsub_rn(__dadd_rn(m0, log(s0)), m1), log(s1));
-        } else {
-          out[t] = (T)__dsub_rn(m0, m1);
-        }
-      }
+      double nre, nim;
+      complex_gaussian_f64(r, nre, nim);
+      const int li = lab[s];
+      const double yre = __dadd_rn(pts[2 * li], __dmul_rn(nre, sd));
+      const double yim = __dadd_rn(pts[2 * li + 1], __dmul_rn(nim, sd));
+      const int t0 = s * a.mbits;
+      demap_f64(pts, a.m, a.mbits, a.log_m, a.exact != 0, yre, yim, sigma2, c.e - t0,
+                [&](int o, double v) { out[t0 + o] = (T)v; });
     }
   } else {
     const float sd = (float)__dsqrt_rn(sigma2);

@@ -229,6 +229,48 @@ size_t accumulate_encode_smem(int k, int m);
 cudaError_t launch_sums_encode(const SumsEncodeArgs& a, cudaStream_t stream);
 cudaError_t launch_accumulate_encode(const AccumulateEncodeArgs& a, cudaStream_t stream);
 
+// ---- the link of a specification over a generic code (link.cu)
+struct LinkRecord {
+  uint32_t raw_bit_errors;    // metric ber: uncoded errors of the trial's symbols
+  uint32_t coded_bit_errors;  // metric coded_ber: errors of the decoded payload
+  uint32_t block_errors;      // metric bler: blocks with an error
+  uint32_t iterations;        // decoder iterations summed over the blocks
+};
+struct LinkGenArgs {
+  int32_t k, n, blocks, rank;
+  const int32_t* info_pos;   // k
+  const int32_t* pivots;     // rank
+  const uint32_t* pmat;      // ceil(k/32) x rank, word-major
+  const int32_t* perm;       // n x blocks interleaver (null: none)
+  int32_t m, mbits, n_pad, bits_per_chunk, syms_per_chunk;
+  const double* points;      // [2 m]
+  double log_m, b_ebn0;
+  int32_t exact;
+  const uint64_t* jumps;     // [2 threads + 1][4]
+  // the grid slicer of the metric ber
+  int32_t side;
+  double step, re0, im0;
+  const int32_t* lookup;     // [m]: the label of cell (row, col) at row * side + col
+  uint64_t seed, name_hash, cond, first_trial;
+  int64_t n_trials;
+  double* llr_out;           // [n_trials][n x blocks], deinterleaved
+  uint32_t* payload_out;     // [n_trials][blocks][ceil(k/32)]
+  uint32_t* raw_errors_out;  // [n_trials]
+};
+struct LinkCountArgs {
+  int32_t k, n, blocks;
+  const int32_t* info_pos;
+  const double* post;        // [n_trials x blocks][n]
+  const int32_t* iters;      // [n_trials x blocks]
+  const uint32_t* payload;   // [n_trials][blocks][ceil(k/32)]
+  const uint32_t* raw_errors;
+  int64_t n_trials;
+  LinkRecord* out;
+};
+size_t link_gen_smem_bytes(int m, int mbits, int k, int n, int blocks, int n_pad);
+cudaError_t launch_link_gen(const LinkGenArgs& a, cudaStream_t stream);
+cudaError_t launch_link_count(const LinkCountArgs& a, cudaStream_t stream);
+
 // ---- the NR code through the generic decoder (nr_generic.cu)
 template <typename T>
 struct NrEpilogueArgs {

@@ -1,0 +1,61 @@
+// The f64 channel of the frame generators: one complex Gaussian sample of the
+// reference's generator and the LLRs of one received QAM symbol.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "crmath.cuh"
+#include "device_common.cuh"
+
+namespace cbk {
+
+// Rng::complex_gaussian (crates/com-core/src/rng.rs:161-167): two uniforms u1, u2;
+// r = sqrt(-2 ln(1 - u1)) / sqrt(2); (r cos 2 pi u2, r sin 2 pi u2), with the correctly
+// rounded log, sin and cos of crmath.cuh
+__device__ __forceinline__ void complex_gaussian_f64(cbd::Xoshiro& r, double& nre, double& nim) {
+  const double u1 = (double)(cbd::xoshiro_next(r) >> 11) * (1.0 / 9007199254740992.0);
+  const double u2 = (double)(cbd::xoshiro_next(r) >> 11) * (1.0 / 9007199254740992.0);
+  const double l = crm::cr_log(__dsub_rn(1.0, u1));
+  const double rad = __dmul_rn(__dsqrt_rn(__dmul_rn(-2.0, l)), 0.70710678118654752440);
+  double sn, cs;
+  crm::cr_sincos(__dmul_rn(6.283185307179586, u2), &sn, &cs);
+  nre = __dmul_rn(rad, cs);
+  nim = __dmul_rn(rad, sn);
+}
+
+// The LLRs of the mbits bits of one symbol y, most significant first
+// (crates/com-mapping/src/demapper.rs:82-146, :270-297): metric_i = -|y - x_i|^2 /
+// sigma^2 - ln M; max-log L = max_{b=0} - max_{b=1}; exact (LabelHalves) the sums of
+// exp(metric - max) in label order, L = m0 + ln s0 - m1 - ln s1, with CUDA's exp and
+// log where the reference calls libm.  put(o, L) receives bit o's LLR; bits at o >=
+// n_bits are skipped.
+template <typename Put>
+__device__ __forceinline__ void demap_f64(const double* pts, int m, int mbits, double log_m, bool exact, double yre,
+                                          double yim, double sigma2, int n_bits, Put&& put) {
+  const double uniform = -log_m;
+  for (int o = 0; o < mbits && o < n_bits; o++) {
+    const int shift = mbits - 1 - o;
+    double m0 = -INFINITY, m1 = -INFINITY;
+    for (int i = 0; i < m; i++) {
+      const double dr = __dsub_rn(yre, pts[2 * i]), di = __dsub_rn(yim, pts[2 * i + 1]);
+      const double ns = __dadd_rn(__dmul_rn(dr, dr), __dmul_rn(di, di));
+      const double met = __dadd_rn(__ddiv_rn(-ns, sigma2), uniform);
+      if ((i >> shift) & 1) m1 = fmax(m1, met);
+      else m0 = fmax(m0, met);
+    }
+    if (exact && isfinite(m0) && isfinite(m1)) {
+      double s0 = 0.0, s1 = 0.0;
+      for (int i = 0; i < m; i++) {
+        const double dr = __dsub_rn(yre, pts[2 * i]), di = __dsub_rn(yim, pts[2 * i + 1]);
+        const double ns = __dadd_rn(__dmul_rn(dr, dr), __dmul_rn(di, di));
+        const double met = __dadd_rn(__ddiv_rn(-ns, sigma2), uniform);
+        if ((i >> shift) & 1) s1 = __dadd_rn(s1, exp(__dsub_rn(met, m1)));
+        else s0 = __dadd_rn(s0, exp(__dsub_rn(met, m0)));
+      }
+      put(o, __dsub_rn(__dsub_rn(__dadd_rn(m0, log(s0)), m1), log(s1)));
+    } else {
+      put(o, __dsub_rn(m0, m1));
+    }
+  }
+}
+
+}  // namespace cbk

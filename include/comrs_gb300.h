@@ -274,6 +274,48 @@ cb_status cb_ldpc_encode_device(cb_ldpc* code, const uint8_t* info_dev, int64_t 
  * were linked (the reference's rows, hence its alist files). */
 cb_status cb_ldpc_peg(int32_t n, int32_t k, int32_t var_degree, uint64_t seed, int32_t* row_start, int32_t* vars);
 
+/* ---- The link of a com-spec specification over a generic code: the blocks
+ * fec_encode -> map -> awgn_ebn0 -> demap -> fec_decode of a Link (crates/com-spec/src/
+ * link.rs:109-124) as specs/bicm_ldpc.yaml chains them, one trial per call unit:
+ *   fec_encode (blocks/coding/fec.rs:60-78): k x blocks payload bits drawn with Rng::bit,
+ *     every block encoded (the from_rows encoder), the codewords one after the other,
+ *     then, when `interleave` is set, Interleaver::random(n x blocks, interleaver_seed);
+ *   map (blocks/coding/map.rs:31-47): padding bits to a multiple of log2 M, Gray QAM;
+ *   awgn_ebn0 (blocks/channel.rs:141-156): the measured mean power, b = log2 M k / n;
+ *   demap (map.rs:55-77): exact (exact_demap = 1, the block's default) or max-log LLRs;
+ *   fec_decode (fec.rs:88-102): deinterleave, decode every block with the code's decoder.
+ * Trial t of condition c draws from stream(seed, name, c, t).  Per trial the counts of
+ * the metrics (crates/com-spec/src/metrics.rs:254-351): ber (uncoded decisions of the
+ * power-scaled samples by the grid slicer), coded_ber, bler.  The code object must be
+ * f64 with the CB_ENC_SUMS encoder, and outlive the link; both are used under their
+ * locks. */
+typedef struct {
+  uint32_t raw_bit_errors;   /* ber: errors of the n_sym log2 M sent bits */
+  uint32_t coded_bit_errors; /* coded_ber: errors of the k x blocks payload bits */
+  uint32_t block_errors;     /* bler: blocks with an error */
+  uint32_t iterations;       /* decoder iterations summed over the blocks */
+} cb_link_record;
+typedef struct cb_link cb_link;
+cb_status cb_link_create(cb_ldpc* code, int32_t blocks, int32_t modulation_order, int32_t interleave,
+                         uint64_t interleaver_seed, int32_t exact_demap, cb_link** out);
+void cb_link_destroy(cb_link* link);
+const char* cb_link_last_error(const cb_link* link);
+/* info[0..8): k, n, blocks, M, sent bits per trial (n x blocks + padding), payload bits
+ * per trial, padding bits, 1 if interleaved */
+cb_status cb_link_info(const cb_link* link, int64_t info[8]);
+/* the interleaver's permutation perm[n x blocks]: stream bit t is coded bit perm[t]
+ * (Interleaver::perm, crates/com-fec/src/interleaving.rs:52-55); host only */
+cb_status cb_link_interleaver(const cb_link* link, int32_t* perm);
+/* trials [first_trial, first_trial + n_trials) of one condition; records in trial order
+ * into `out` (host) */
+cb_status cb_link_run_trials(cb_link* link, uint64_t seed, uint64_t name_hash, uint64_t condition,
+                             uint64_t first_trial, int64_t n_trials, double ebn0_db, cb_link_record* out);
+/* the same trials' decoder inputs: llr [n_trials][n x blocks] (deinterleaved), payload
+ * [n_trials][k x blocks] bytes and the uncoded bit errors [n_trials] (each nullable) */
+cb_status cb_link_generate(cb_link* link, uint64_t seed, uint64_t name_hash, uint64_t condition,
+                           uint64_t first_trial, int64_t n_trials, double ebn0_db, double* llr, uint8_t* payload,
+                           uint32_t* raw_errors);
+
 /* cb_decode_device for callers that cannot allocate device memory (a host framework
  * that owns all device memory through its own pool, or a real-time loop that forbids
  * cudaMalloc after start-up).  No counterpart in the reference: it is an addition of

@@ -93,6 +93,15 @@ struct Rng {
   double uniform() { return (double)(next_u64() >> 11) * (1.0 / 9007199254740992.0); }
   // rng.rs:146-148
   uint8_t bit() { return (uint8_t)(next_u64() >> 63); }
+  // rng.rs:125-128
+  uint64_t below(uint64_t n) {
+    uint64_t v = (uint64_t)(uniform() * (double)n);
+    return std::min(v, n - 1);
+  }
+  // rng.rs:218-222
+  void shuffle(std::vector<int32_t>& v) {
+    for (size_t i = v.size(); i-- > 1;) std::swap(v[i], v[below(i + 1)]);
+  }
   // rng.rs:152-157
   double gaussian() {
     double u1 = uniform(), u2 = uniform();
@@ -716,6 +725,140 @@ static void encode_sums(const Code& c, const uint8_t* u, uint8_t* cw) {
   }
 }
 
+// ------------------------------------------------------------------ spec link
+// The link fec_encode -> map -> awgn_ebn0 -> demap -> fec_decode of a com-spec
+// specification over a generic LdpcCode (the PEG code of specs/bicm_ldpc.yaml), with
+// its metrics:
+//   Encode::apply (crates/com-spec/src/blocks/coding/fec.rs:60-78): k x blocks bits,
+//   the blocks' codewords one after the other, then Interleaver::random(len, seed)
+//   (crates/com-fec/src/interleaving.rs:63-67, out[i] = in[perm[i]]);
+//   Map and Demap (blocks/coding/map.rs:31-77); AwgnEbn0 (blocks/channel.rs:141-156,
+//   b = log2 M k / n, block.rs:59-61);
+//   Decode::apply (fec.rs:88-102): deinterleave (x[perm[i]] = y[i]), decode every block,
+//   hard decisions at the information positions (ldpc.rs:793-796);
+//   ber: the samples scaled by sqrt(energy(x) / energy(y)), the grid slicer's decisions
+//   against the sent bits (crates/com-spec/src/metrics.rs:254-284, :374-383,
+//   crates/com-math/src/nearest.rs); coded_ber and bler (metrics.rs:334-351).
+
+static std::vector<int32_t> random_perm(int n, uint64_t seed) {
+  std::vector<int32_t> perm(n);
+  for (int i = 0; i < n; i++) perm[i] = i;
+  Rng r(seed);
+  r.shuffle(perm);
+  return perm;
+}
+
+// nearest.rs Slicer::detect for a square QAM: the levels of each axis (sorted, equal
+// within 1e-9 of the span merged), the step of the real levels, a lookup by cell
+struct GridSlicer {
+  int side = 0;
+  double step = 0, re0 = 0, im0 = 0;
+  std::vector<int> lookup;
+};
+
+static std::vector<double> axis_levels(std::vector<double> l) {
+  std::sort(l.begin(), l.end());
+  double span = std::max(std::fabs(l.back() - l[0]), 1e-300);
+  std::vector<double> out;
+  for (double v : l)
+    if (out.empty() || std::fabs(out.back() - v) > 1e-9 * span) out.push_back(v);
+  return out;
+}
+
+static GridSlicer grid_slicer(const Qam& q) {
+  GridSlicer g;
+  std::vector<double> re = axis_levels(q.re), im = axis_levels(q.im);
+  g.side = (int)re.size();
+  g.step = (re.back() - re[0]) / (double)(g.side - 1);
+  g.re0 = re[0];
+  g.im0 = im[0];
+  g.lookup.assign(q.m, 0);
+  for (int i = 0; i < q.m; i++) {
+    int c = (int)std::round((q.re[i] - re[0]) / g.step), r = (int)std::round((q.im[i] - im[0]) / g.step);
+    g.lookup[r * g.side + c] = i;
+  }
+  return g;
+}
+
+static int grid_cell(const GridSlicer& g, double x, double x0) {
+  double c = std::round((x - x0) / g.step);
+  return (int)std::min(std::max(c, 0.0), (double)(g.side - 1));
+}
+
+struct LinkCounts {
+  int64_t raw_errors, raw_bits, coded_errors, coded_bits, block_errors, blocks, iterations;
+};
+
+static LinkCounts link_trial(const Code& c, const Qam& q, const GridSlicer& g, int blocks,
+                             const std::vector<int32_t>* perm, Rng& rng, double ebn0_db, NoiseMode mode,
+                             double* llr_out, uint8_t* payload_out) {
+  const int k = c.k, n = c.n, mb = q.bits, nb = n * blocks;
+  std::vector<uint8_t> u((size_t)k * blocks), coded(nb);
+  for (auto& b : u) b = rng.bit();  // fec.rs:63
+  for (int b = 0; b < blocks; b++) {
+    if (c.accumulate) encode_accumulate(c, &u[(size_t)b * k], &coded[(size_t)b * n]);
+    else encode_sums(c, &u[(size_t)b * k], &coded[(size_t)b * n]);
+  }
+  std::vector<uint8_t> bits(nb);
+  for (int i = 0; i < nb; i++) bits[i] = perm ? coded[(*perm)[i]] : coded[i];
+  while ((int)bits.size() % mb != 0) bits.push_back(rng.bit());  // map.rs:36-38
+  const int ns = (int)bits.size() / mb;
+  std::vector<double> xr(ns), xi(ns), yr(ns), yi(ns);
+  for (int s = 0; s < ns; s++) {
+    int idx = 0;
+    for (int b = 0; b < mb; b++) idx = (idx << 1) | (bits[(size_t)s * mb + b] & 1);
+    xr[s] = q.re[idx];
+    xi[s] = q.im[idx];
+  }
+  double ex = 0.0;
+  for (int s = 0; s < ns; s++) ex += xr[s] * xr[s] + xi[s] * xi[s];
+  double p = (0.0 + ex) / (double)ns;
+  double rate = (double)k / (double)n;
+  double sigma2 = p * 1.0 / ((double)mb * rate * db2lin(ebn0_db));
+  double sd = std::sqrt(sigma2);
+  for (int s = 0; s < ns; s++) {
+    double nr, ni;
+    rng.complex_gaussian(nr, ni, mode);
+    yr[s] = xr[s] + nr * sd;
+    yi[s] = xi[s] + ni * sd;
+  }
+  std::vector<double> llr((size_t)ns * mb);
+  for (int s = 0; s < ns; s++) {
+    if (c.exact_demap) demap_exact(q, yr[s], yi[s], sigma2, &llr[(size_t)s * mb]);
+    else demap_maxlog(q, yr[s], yi[s], sigma2, &llr[(size_t)s * mb]);
+  }
+  LinkCounts r{};
+  // ber: energy(x) and energy(y) over the window (every symbol), g = sqrt(px / pz)
+  double ey = 0.0;
+  for (int s = 0; s < ns; s++) ey += yr[s] * yr[s] + yi[s] * yi[s];
+  double ex0 = 0.0 + ex, ey0 = 0.0 + ey;
+  double gain = ey0 > 0.0 ? std::sqrt(ex0 / ey0) : 1.0;
+  for (int s = 0; s < ns; s++) {
+    double zr = yr[s] * gain, zi = yi[s] * gain;
+    int lab = g.lookup[grid_cell(g, zi, g.im0) * g.side + grid_cell(g, zr, g.re0)];
+    for (int b = 0; b < mb; b++) r.raw_errors += ((lab >> (mb - 1 - b)) & 1) != bits[(size_t)s * mb + b];
+  }
+  r.raw_bits = (int64_t)ns * mb;
+  // fec_decode: the first n x blocks LLRs, deinterleaved, block by block
+  std::vector<double> dl(nb), post(n);
+  for (int i = 0; i < nb; i++) {
+    if (perm) dl[(*perm)[i]] = llr[i];
+    else dl[i] = llr[i];
+  }
+  for (int b = 0; b < blocks; b++) {
+    std::copy(&dl[(size_t)b * n], &dl[(size_t)b * n] + n, post.begin());
+    r.iterations += propagate<double>(c, &dl[(size_t)b * n], post.data());
+    int e = 0;
+    for (int i = 0; i < k; i++) e += (uint8_t)(post[c.info[i]] < 0.0) != u[(size_t)b * k + i];
+    r.coded_errors += e;
+    r.block_errors += e > 0;
+  }
+  r.coded_bits = (int64_t)k * blocks;
+  r.blocks = blocks;
+  if (llr_out) std::memcpy(llr_out, dl.data(), sizeof(double) * nb);
+  if (payload_out) std::memcpy(payload_out, u.data(), u.size());
+  return r;
+}
 
 // ------------------------------------------------------------------ learned min-sum
 // Test oracle of this project's neural min-sum (no counterpart in the reference): the
@@ -1103,6 +1246,52 @@ int64_t or_learned_num_weights(void* h, int T, int shared) {
   std::vector<int> ls;
   learned_layers(*c, ls);
   return (int64_t)T * ls.back() * (shared ? 1 : c->z);
+}
+
+// Trials [first, first + n) of the spec link over a generic code (from_rows or
+// accumulate) with `blocks` codewords per trial, the random interleaver of seed
+// `il_seed` (il_seed < 0: none), M-QAM, the demapper of or_code_set_demapper and the
+// code's decoder; 7 counts per trial into out (raw errors, raw bits, coded errors,
+// coded bits, block errors, blocks, iterations); optionally the deinterleaved LLRs
+// [n][blocks x n] and the payload bits [n][blocks x k].
+int or_link_trials(void* h, int blocks, int64_t il_seed, int m, uint64_t seed, uint64_t name_hash, uint64_t cond,
+                   uint64_t first, uint64_t n, double ebn0_db, int noise, int threads, int64_t* out, double* llr_out,
+                   uint8_t* payload_out) {
+  Code* c = (Code*)h;
+  Qam q;
+  if (!qam_new(m, q)) return -1;
+  GridSlicer g = grid_slicer(q);
+  std::vector<int32_t> perm;
+  if (il_seed >= 0) perm = random_perm(c->n * blocks, (uint64_t)il_seed);
+  if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  std::atomic<uint64_t> next(0);
+  auto work = [&]() {
+    for (;;) {
+      uint64_t i = next.fetch_add(1);
+      if (i >= n) break;
+      Rng rng = stream(seed, name_hash, cond, first + i);
+      LinkCounts r = link_trial(*c, q, g, blocks, il_seed >= 0 ? &perm : nullptr, rng, ebn0_db, (NoiseMode)noise,
+                                llr_out ? llr_out + i * (size_t)c->n * blocks : nullptr,
+                                payload_out ? payload_out + i * (size_t)c->k * blocks : nullptr);
+      int64_t* o = out + 7 * i;
+      o[0] = r.raw_errors; o[1] = r.raw_bits; o[2] = r.coded_errors; o[3] = r.coded_bits;
+      o[4] = r.block_errors; o[5] = r.blocks; o[6] = r.iterations;
+    }
+  };
+  if (threads == 1) {
+    work();
+  } else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++) pool.emplace_back(work);
+    for (auto& t : pool) t.join();
+  }
+  return 0;
+}
+
+// Interleaver::random(n, seed)
+void or_random_perm(int n, uint64_t seed, int32_t* out) {
+  std::vector<int32_t> p = random_perm(n, seed);
+  std::memcpy(out, p.data(), sizeof(int32_t) * n);
 }
 
 }  // extern "C"

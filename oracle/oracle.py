@@ -48,6 +48,10 @@ def lib():
         L.or_code_from_rows.restype = vp
         L.or_code_from_rows.argtypes = [i32, i32, vp, vp, i32, C.c_char_p, i32]
         L.or_code_info_positions.argtypes = [vp, vp]
+        L.or_link_trials.restype = i32
+        L.or_link_trials.argtypes = [vp, i32, C.c_int64, i32, u64, u64, u64, u64, u64, C.c_double, i32, i32, vp, vp,
+                                     vp]
+        L.or_random_perm.argtypes = [i32, u64, vp]
         L.or_code_free.argtypes = [vp]
         L.or_code_info.argtypes = [vp, vp]
         L.or_code_bit_map.argtypes = [vp, vp]
@@ -106,6 +110,13 @@ def complex_gaussians(seed, n, mode=NOISE_LIBM):
     re, im = np.zeros(n), np.zeros(n)
     lib().or_complex_gaussians(seed, n, mode, _p(re), _p(im))
     return re, im
+
+
+def random_perm(n, seed):
+    """Interleaver::random(n, seed).perm()"""
+    out = np.zeros(n, np.int32)
+    lib().or_random_perm(n, seed, _p(out))
+    return out
 
 
 def qam(m):
@@ -187,6 +198,22 @@ class Code:
         out = np.zeros(self.k, np.int32)
         lib().or_code_info_positions(self.h, _p(out))
         return out
+
+    def link_trials(self, blocks, interleaver_seed, m, seed, name_hash, cond, first, n, ebn0_db, noise=NOISE_CR,
+                    threads=0, want_llr=False, want_payload=False):
+        """Trials of the spec link fec_encode -> map -> awgn_ebn0 -> demap -> fec_decode
+        (interleaver_seed None: no interleaver): counts [n][7] = raw errors, raw bits,
+        coded errors, coded bits, block errors, blocks, iterations; optionally the
+        deinterleaved LLRs and the payload bits."""
+        out = np.zeros((n, 7), np.int64)
+        llr = np.zeros((n, blocks * self.n_full)) if want_llr else None
+        pay = np.zeros((n, blocks * self.k), np.uint8) if want_payload else None
+        il = -1 if interleaver_seed is None else int(interleaver_seed)
+        st = lib().or_link_trials(self.h, blocks, il, m, seed, name_hash, cond, first, n, ebn0_db, noise, threads,
+                                  _p(out), _p(llr), _p(pay))
+        if st != 0:
+            raise ValueError(f"modulation order {m}")
+        return out, llr, pay
 
     def encode_full(self, u):
         u = np.ascontiguousarray(u, np.uint8)
