@@ -17,6 +17,12 @@ records returned to pinned host memory every step; `roofline` = the decoder kern
 against the measured HBM copy bandwidth.
 --impl reference: the CPU oracle's restatement of the reference trial (f64, the
 reference's libm noise) on all host cores, a bounded sample of frames per step.
+
+--workload spec: the link of com-rs's specs/bicm_ldpc.yaml instead (fec_encode of a PEG
+(1024, 512) code, 8 blocks per trial, random interleaver, Gray 16-QAM, awgn_ebn0, exact
+LLRs, layered sum-product with 50 iterations, f64), Eb/N0 2.5:0.5:5 dB, `--trials` trials
+per step; step s runs grid point s mod 6.  Same keys; the roofline is the generic
+decoder kernel against HBM (it is FP64-bound: the sum-product rule's tanh and atanh).
 """
 
 import argparse
@@ -282,6 +288,187 @@ def run_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+SPEC_N, SPEC_K, SPEC_BLOCKS, SPEC_M = 1024, 512, 8, 16
+SPEC_GRID = [2.5 + 0.5 * i for i in range(6)]
+SPEC_SEED, SPEC_NAME = 6, "bicm_ldpc"
+SPEC_METRIC = "decoded info Gbit/s of the bicm_ldpc specification's link; vs CPU Runner"
+SPEC_WORKLOAD = ("specs/bicm_ldpc.yaml link: PEG(1024, 512) var degree 3 seed 1, 8 blocks per trial, random "
+                 "interleaver, Gray 16-QAM, AWGN Eb/N0 2.5:0.5:5 dB, exact LLRs, layered sum-product <= 50 "
+                 "iterations + syndrome stop, f64")
+# algorithmic bytes of one decoded codeword through cb_ldpc_decode_device: n f64 LLRs in,
+# n f64 posteriors out, a 4-byte iteration count
+SPEC_ALGO_BYTES = SPEC_N * 8 * 2 + 4
+
+
+def spec_cpu_sample(steps, warmup, threads=0, budget_s=2.0):
+    """The oracle's spec link (f64, libm noise, as the reference) over all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    cb = importlib.import_module("com-rs_gb300")
+    cores = threads or os.cpu_count()
+    code = O.Code(rows=cb.ldpc.peg_rows(SPEC_N, SPEC_K), n=SPEC_N).set_decoder(O.RULE_SUM_PRODUCT, 0.8, True, 50)
+    code.set_demapper(True)
+    h = O.fnv1a64(SPEC_NAME)
+
+    def trials(cond, first, n):
+        return code.link_trials(SPEC_BLOCKS, 0, SPEC_M, SPEC_SEED, h, cond, first, n, SPEC_GRID[cond],
+                                O.NOISE_LIBM, cores)[0]
+
+    t0 = time.perf_counter()
+    trials(0, 0, cores)
+    per = (time.perf_counter() - t0) / cores
+    n = max(cores, int(budget_s / per / cores) * cores)
+    for s in range(warmup):
+        trials(s % 6, 10_000_000 + s * n, n)
+    total_t, done, be = 0.0, 0, 0
+    for s in range(steps):
+        t0 = time.perf_counter()
+        out = trials(s % 6, (s // 6) * n, n)
+        total_t += time.perf_counter() - t0
+        done += n
+        be += int(out[:, 4].sum())
+    gbps = done * SPEC_BLOCKS * SPEC_K / total_t / 1e9
+    return gbps, cores, n, done, total_t, be / (done * SPEC_BLOCKS)
+
+
+def run_spec_reference(args, rank):
+    if rank != 0:
+        return
+    gbps, cores, n, done, t, bler = spec_cpu_sample(args.steps, args.warmup)
+    sample = (f"{n} trials per step ({done} in {args.steps} steps, {t:.1f} s) of the same link, f64 with libm "
+              f"noise and libm tanh/atanh as the reference")
+    line = {"impl": "reference", "metric": SPEC_METRIC, "value": gbps, "unit": "Gbit/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": SPEC_WORKLOAD, "trials_per_step": n, "bler": bler},
+            "cpu_baseline": {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": gbps, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_spec_ours(args, rank, world, local_rank):
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    cb = importlib.import_module("com-rs_gb300")
+    L = cb.lib()
+    T = args.trials
+    code = cb.Ldpc.peg(SPEC_N, SPEC_K, rule="sum_product", max_iterations=50, device=local_rank)
+    link = cb.Link(code, SPEC_BLOCKS, SPEC_M, True, 0, "exact")
+    nh = cb.fnv1a64(SPEC_NAME)
+    rec = torch.empty(T * 16, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def step(s):
+        cond = s % 6
+        first = (s // 6) * T * world + rank * T
+        st = L.cb_link_run_trials_device(link._h, SPEC_SEED, nh, cond, first, T, SPEC_GRID[cond],
+                                         C.c_void_p(rec.data_ptr()), sp)
+        if st:
+            raise cb.ComrsError(st, L.cb_link_last_error(link._h).decode())
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for s in range(args.warmup):
+        step(10_000 + s)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        ev0.record(stream)
+        for s in range(args.steps):
+            step(s)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = max_over_ranks(ev0.elapsed_time(ev1))
+    last = rec.cpu().numpy().view(cb.LINK_DTYPE)
+    value = args.steps * T * world * SPEC_BLOCKS * SPEC_K / (ms * 1e-3) / 1e9
+
+    # roofline of the decoder kernel: one step's LLRs in HBM, CUDA events around the decode
+    llr_h, _, _ = link.generate(SPEC_SEED, SPEC_NAME, 0, 3_000_000, T, SPEC_GRID[0])
+    llr = torch.from_numpy(llr_h).cuda()
+    post = torch.empty_like(llr)
+    iters = torch.empty(T * SPEC_BLOCKS, dtype=torch.int32, device="cuda")
+    dec_ms = []
+    for rep in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = L.cb_ldpc_decode_device(code._h, C.c_void_p(llr.data_ptr()), T * SPEC_BLOCKS,
+                                     C.c_void_p(post.data_ptr()), C.c_void_p(iters.data_ptr()), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if st:
+            raise cb.ComrsError(st, L.cb_ldpc_last_error(code._h).decode())
+        if rep:
+            dec_ms.append(e0.elapsed_time(e1))
+    dec = float(np.mean(dec_ms))
+    achieved = T * SPEC_BLOCKS * SPEC_ALGO_BYTES / (dec * 1e-3) / 1e9
+    peaks = read_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "sparse_kernel<double, sum-product, layered> (generic decoder)",
+                "algorithmic_bytes_per_launch": T * SPEC_BLOCKS * SPEC_ALGO_BYTES, "launch_ms": dec,
+                "mean_iterations": float(iters.float().mean()),
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+                "note": "FP64-bound (tanh/atanh per edge), not HBM-bound"}
+
+    # end to end through the public C ABI: records to pinned host memory
+    host = torch.empty(T * 16, dtype=torch.uint8, pin_memory=True)
+    out_p = C.c_void_p(host.data_ptr())
+    L.cb_link_run_trials(link._h, SPEC_SEED, nh, 0, 4_000_000, T, SPEC_GRID[0], out_p)
+    barrier()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        cond = s % 6
+        first = (s // 6) * T * world + rank * T
+        st = L.cb_link_run_trials(link._h, SPEC_SEED, nh, cond, first, T, SPEC_GRID[cond], out_p)
+        if st:
+            raise cb.ComrsError(st, L.cb_link_last_error(link._h).decode())
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = {"value": args.steps * T * world * SPEC_BLOCKS * SPEC_K / e2e_s / 1e9, "unit": "Gbit/s",
+           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": T * 16, "api": "cb_link_run_trials (host records)",
+           "inputs": "the trials' streams (seed, name, condition, trial index) passed as arguments"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        gbps, cores, n, done, t, _ = spec_cpu_sample(2, 0, budget_s=5.0)
+        cpu = {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port",
+               "sample": f"{done} trials ({t:.1f} s) of the same link at 2.5 and 3 dB, f64 with libm noise and "
+                         f"libm tanh/atanh as the reference"}
+    if rank == 0:
+        line = {"metric": SPEC_METRIC, "value": value, "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (Monte Carlo trials from seeded streams)",
+                "config": {"workload": SPEC_WORKLOAD, "trials_per_step": T, "codewords_per_step": T * SPEC_BLOCKS,
+                           "ebn0_db": SPEC_GRID,
+                           "l2": "inputs larger than L2: each step writes and reads 134 MB of f64 LLRs at 2048 trials",
+                           "parallelism": f"dp{world} (disjoint trial ranges per GPU)",
+                           "last_step_bler": float(last["block_errors"].sum()) / (T * SPEC_BLOCKS)},
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
+                "gpu_launches": 3 * args.steps}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def run_profile_case(args):
     """The small case the committed ncu summaries capture: `frames` C2 codewords generated
     once (Eb/N0 = 1 dB), then decoded three times."""
@@ -315,6 +502,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--frames", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", choices=["c2", "spec"], default="c2",
+                    help="c2: the NR trial (the headline); spec: the link of specs/bicm_ldpc.yaml")
+    ap.add_argument("--trials", type=int, default=2048, help="trials per step of --workload spec")
     ap.add_argument("--profile-case", action="store_true",
                     help="generate --frames C2 codewords and decode them three times (for ncu)")
     args = ap.parse_args()
@@ -324,7 +514,12 @@ def main():
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
-    if args.impl == "reference":
+    if args.workload == "spec":
+        if args.impl == "reference":
+            run_spec_reference(args, rank)
+        else:
+            run_spec_ours(args, rank, world, local_rank)
+    elif args.impl == "reference":
         run_reference(args, rank)
     else:
         run_ours(args, rank, world, local_rank)

@@ -112,6 +112,7 @@ SYMBOLS = [
     ("cb_link_info", _i32, [_vp, _vp]),
     ("cb_link_interleaver", _i32, [_vp, _vp]),
     ("cb_link_run_trials", _i32, [_vp, _u64, _u64, _u64, _u64, _i64, _dbl, _vp]),
+    ("cb_link_run_trials_device", _i32, [_vp, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp]),
     ("cb_link_generate", _i32, [_vp, _u64, _u64, _u64, _u64, _i64, _dbl, _vp, _vp, _vp]),
 ]
 

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -374,7 +375,7 @@ cb_status link_ensure_device(cb_link* l) {
 // trials [first, first + n) into the link's device buffers: generation, decoding and,
 // when `count` is set, the records
 cb_status link_run_device(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first, int64_t n,
-                          double ebn0_db, bool count) {
+                          double ebn0_db, bool count, cudaStream_t s, cbk::LinkRecord* out_dev = nullptr) {
   cb_ldpc* c = l->code;
   const cbh::SparseEncoder& e = c->enc;
   const int nb = c->host.n * l->blocks, wk = (e.k + 31) / 32;
@@ -418,9 +419,9 @@ cb_status link_run_device(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_
   a.llr_out = (double*)l->d_llr;
   a.payload_out = (uint32_t*)l->d_payload;
   a.raw_errors_out = (uint32_t*)l->d_raw;
-  LINK_CUDA(l, cbk::launch_link_gen(a, c->stream));
+  LINK_CUDA(l, cbk::launch_link_gen(a, s));
   if (cb_status st = decode_impl<double>(c, (const double*)l->d_llr, n * l->blocks, (double*)l->d_post,
-                                         (int32_t*)l->d_iters, c->stream))
+                                         (int32_t*)l->d_iters, s))
     return kfail(l, st, c->err);
   if (count) {
     cbk::LinkCountArgs ca;
@@ -433,8 +434,8 @@ cb_status link_run_device(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_
     ca.payload = (const uint32_t*)l->d_payload;
     ca.raw_errors = (const uint32_t*)l->d_raw;
     ca.n_trials = n;
-    ca.out = (cbk::LinkRecord*)l->d_rec;
-    LINK_CUDA(l, cbk::launch_link_count(ca, c->stream));
+    ca.out = out_dev ? out_dev : (cbk::LinkRecord*)l->d_rec;
+    LINK_CUDA(l, cbk::launch_link_count(ca, s));
   }
   return CB_OK;
 }
@@ -747,12 +748,31 @@ cb_status cb_link_run_trials(cb_link* l, uint64_t seed, uint64_t name_hash, uint
   const int64_t chunk = link_chunk(l, n_trials);
   for (int64_t f0 = 0; f0 < n_trials; f0 += chunk) {
     const int64_t cnt = std::min(chunk, n_trials - f0);
-    if (cb_status st = link_run_device(l, seed, name_hash, condition, first_trial + f0, cnt, ebn0_db, true)) return st;
+    if (cb_status st = link_run_device(l, seed, name_hash, condition, first_trial + f0, cnt, ebn0_db, true,
+                                       l->code->stream))
+      return st;
     LINK_CUDA(l, cudaMemcpyAsync(out + f0, l->d_rec, cnt * sizeof(cb_link_record), cudaMemcpyDeviceToHost,
                                  l->code->stream));
     LINK_CUDA(l, cudaStreamSynchronize(l->code->stream));
   }
   return CB_OK;
+}
+
+cb_status cb_link_run_trials_device(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_t condition,
+                                    uint64_t first_trial, int64_t n_trials, double ebn0_db, cb_link_record* out_dev,
+                                    void* stream) {
+  if (!l) return kfail(nullptr, CB_ERR_CONFIG, "null link");
+  if (n_trials < 0) return kfail(l, CB_ERR_SHAPE, "n_trials must be >= 0");
+  if (n_trials == 0) return CB_OK;
+  if (!out_dev) return kfail(l, CB_ERR_SHAPE, "null records");
+  std::lock_guard<std::mutex> lock(l->mu);
+  std::lock_guard<std::mutex> lock_code(l->code->mu);
+  if (cb_status st = link_ensure_device(l)) return st;
+  const int64_t cap = link_chunk(l, INT64_MAX);
+  if (n_trials > cap) return kfail(l, CB_ERR_SHAPE, "at most " + std::to_string(cap) + " trials per device call");
+  return link_run_device(l, seed, name_hash, condition, first_trial, n_trials, ebn0_db, true,
+                         stream ? (cudaStream_t)stream : l->code->stream,
+                         reinterpret_cast<cbk::LinkRecord*>(out_dev));
 }
 
 cb_status cb_link_generate(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_t condition, uint64_t first_trial,
@@ -768,7 +788,8 @@ cb_status cb_link_generate(cb_link* l, uint64_t seed, uint64_t name_hash, uint64
   std::vector<uint32_t> words;
   for (int64_t f0 = 0; f0 < n_trials; f0 += chunk) {
     const int64_t cnt = std::min(chunk, n_trials - f0);
-    if (cb_status st = link_run_device(l, seed, name_hash, condition, first_trial + f0, cnt, ebn0_db, false))
+    if (cb_status st = link_run_device(l, seed, name_hash, condition, first_trial + f0, cnt, ebn0_db, false,
+                                       l->code->stream))
       return st;
     cudaStream_t s = l->code->stream;
     if (llr) LINK_CUDA(l, cudaMemcpyAsync(llr + f0 * nb, l->d_llr, cnt * nb * 8, cudaMemcpyDeviceToHost, s));

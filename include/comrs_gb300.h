@@ -310,6 +310,12 @@ cb_status cb_link_interleaver(const cb_link* link, int32_t* perm);
  * into `out` (host) */
 cb_status cb_link_run_trials(cb_link* link, uint64_t seed, uint64_t name_hash, uint64_t condition,
                              uint64_t first_trial, int64_t n_trials, double ebn0_db, cb_link_record* out);
+/* cb_link_run_trials enqueued on `stream` (NULL: the code's stream) with the records in
+ * device memory; the link's scratch holds at most 1 GB of trials per call (CB_ERR_SHAPE
+ * beyond).  Asynchronous: the caller synchronises its stream. */
+cb_status cb_link_run_trials_device(cb_link* link, uint64_t seed, uint64_t name_hash, uint64_t condition,
+                                    uint64_t first_trial, int64_t n_trials, double ebn0_db, cb_link_record* out_dev,
+                                    void* stream);
 /* the same trials' decoder inputs: llr [n_trials][n x blocks] (deinterleaved), payload
  * [n_trials][k x blocks] bytes and the uncoded bit errors [n_trials] (each nullable) */
 cb_status cb_link_generate(cb_link* link, uint64_t seed, uint64_t name_hash, uint64_t condition,
