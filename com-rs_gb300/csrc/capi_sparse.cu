@@ -516,7 +516,7 @@ cb_status cb_ldpc_decode_device(cb_ldpc* c, const void* llr, int64_t n_frames, v
   if (n_frames > 0 && !llr) return lfail(c, CB_ERR_SHAPE, "null LLRs");
   std::lock_guard<std::mutex> lock(c->mu);
   if (cb_status st = ensure_device(c)) return st;
-  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the default stream
   if (c->precision == CB_F64)
     return decode_impl<double>(c, (const double*)llr, n_frames, (double*)post, iterations, s);
   return decode_impl<float>(c, (const float*)llr, n_frames, (float*)post, iterations, s);
@@ -605,7 +605,7 @@ cb_status cb_ldpc_encode_device(cb_ldpc* c, const uint8_t* info, int64_t n_frame
   if (n_frames > 0 && (!info || !coded)) return lfail(c, CB_ERR_SHAPE, "null information or coded bits");
   std::lock_guard<std::mutex> lock(c->mu);
   if (cb_status st = ensure_encoder(c)) return st;
-  return encode_impl(c, info, n_frames, coded, stream ? (cudaStream_t)stream : c->stream);
+  return encode_impl(c, info, n_frames, coded, (cudaStream_t)stream);  // NULL: the default stream
 }
 
 cb_status cb_ldpc_encode(cb_ldpc* c, const uint8_t* info, int64_t n_frames, uint8_t* coded) {
@@ -771,7 +771,7 @@ cb_status cb_link_run_trials_device(cb_link* l, uint64_t seed, uint64_t name_has
   const int64_t cap = link_chunk(l, INT64_MAX);
   if (n_trials > cap) return kfail(l, CB_ERR_SHAPE, "at most " + std::to_string(cap) + " trials per device call");
   return link_run_device(l, seed, name_hash, condition, first_trial, n_trials, ebn0_db, true,
-                         stream ? (cudaStream_t)stream : l->code->stream,
+                         (cudaStream_t)stream,  // NULL: the default stream
                          reinterpret_cast<cbk::LinkRecord*>(out_dev));
 }
 

@@ -237,7 +237,7 @@ cb_status cb_ldpc_levels(const cb_ldpc* code, int32_t* level_start, int32_t* lev
  * posteriors of every frame into `post` and the iterations used into `iterations`
  * (both host, nullable) */
 cb_status cb_ldpc_decode(cb_ldpc* code, const void* llr, int64_t n_frames, void* post, int32_t* iterations);
-/* the same on device buffers, enqueued on `stream` (NULL: the code's own stream) */
+/* the same on device buffers, enqueued on `stream` (cudaStream_t, NULL = default) */
 cb_status cb_ldpc_decode_device(cb_ldpc* code, const void* llr_dev, int64_t n_frames, void* post_dev,
                                 int32_t* iterations_dev, void* stream);
 /* LdpcCode::set_decoder (bindings/com-py/src/fec/ldpc_code.rs:74-86): new decoder
@@ -264,7 +264,7 @@ cb_status cb_ldpc_set_encoder(cb_ldpc* code, int32_t kind, int32_t* k, int32_t* 
  * frame (u8, bit 0 used) into n coded bits per frame (u8); host buffers.  Needs an
  * encoder (cb_ldpc_set_encoder). */
 cb_status cb_ldpc_encode(cb_ldpc* code, const uint8_t* info, int64_t n_frames, uint8_t* coded);
-/* the same on device buffers, enqueued on `stream` (NULL: the code's own stream) */
+/* the same on device buffers, enqueued on `stream` (cudaStream_t, NULL = default) */
 cb_status cb_ldpc_encode_device(cb_ldpc* code, const uint8_t* info_dev, int64_t n_frames, uint8_t* coded_dev,
                                 void* stream);
 /* LdpcCode::peg (ldpc.rs:289-313, :586-634): the rows of a code of n variables and
@@ -310,7 +310,7 @@ cb_status cb_link_interleaver(const cb_link* link, int32_t* perm);
  * into `out` (host) */
 cb_status cb_link_run_trials(cb_link* link, uint64_t seed, uint64_t name_hash, uint64_t condition,
                              uint64_t first_trial, int64_t n_trials, double ebn0_db, cb_link_record* out);
-/* cb_link_run_trials enqueued on `stream` (NULL: the code's stream) with the records in
+/* cb_link_run_trials enqueued on `stream` (cudaStream_t, NULL = default) with the records in
  * device memory; the link's scratch holds at most 1 GB of trials per call (CB_ERR_SHAPE
  * beyond).  Asynchronous: the caller synchronises its stream. */
 cb_status cb_link_run_trials_device(cb_link* link, uint64_t seed, uint64_t name_hash, uint64_t condition,
