@@ -402,6 +402,29 @@ def run_spec_ours(args, rank, world, local_rank):
     last = rec.cpu().numpy().view(cb.LINK_DTYPE)
     value = args.steps * T * world * SPEC_BLOCKS * SPEC_K / (ms * 1e-3) / 1e9
 
+    # the same link with an f32 decoder (the f64 LLRs rounded once to f32)
+    code32 = cb.Ldpc.peg(SPEC_N, SPEC_K, rule="sum_product", max_iterations=50, precision="f32", device=local_rank)
+    link32 = cb.Link(code32, SPEC_BLOCKS, SPEC_M, True, 0, "exact")
+    st = 0
+    for s in range(args.warmup):
+        st |= L.cb_link_run_trials_device(link32._h, SPEC_SEED, nh, s % 6, 20_000_000 + s * T, T, SPEC_GRID[s % 6],
+                                          C.c_void_p(rec.data_ptr()), sp)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in range(args.steps):
+        cond = s % 6
+        st |= L.cb_link_run_trials_device(link32._h, SPEC_SEED, nh, cond, (s // 6) * T * world + rank * T, T,
+                                          SPEC_GRID[cond], C.c_void_p(rec.data_ptr()), sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if st:
+        raise cb.ComrsError(st, L.cb_link_last_error(link32._h).decode())
+    ms32 = max_over_ranks(e0.elapsed_time(e1))
+    f32 = {"value": args.steps * T * world * SPEC_BLOCKS * SPEC_K / (ms32 * 1e-3) / 1e9, "unit": "Gbit/s",
+           "ms_per_step": ms32 / args.steps, "dtype": "f32 decoder on the f64 LLRs rounded once to f32"}
+    link32.close()
+
     # roofline of the decoder kernel: one step's LLRs in HBM, CUDA events around the decode
     llr_h, _, _ = link.generate(SPEC_SEED, SPEC_NAME, 0, 3_000_000, T, SPEC_GRID[0])
     llr = torch.from_numpy(llr_h).cuda()
@@ -463,7 +486,7 @@ def run_spec_ours(args, rank, world, local_rank):
                            "parallelism": f"dp{world} (disjoint trial ranges per GPU)",
                            "last_step_bler": float(last["block_errors"].sum()) / (T * SPEC_BLOCKS)},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
-                "gpu_launches": 3 * args.steps}
+                "gpu_launches": 3 * args.steps, "f32_decoder": f32}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

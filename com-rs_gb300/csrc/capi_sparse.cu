@@ -416,12 +416,16 @@ cb_status link_run_device(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_
   a.cond = cond;
   a.first_trial = first;
   a.n_trials = n;
-  a.llr_out = (double*)l->d_llr;
+  const bool f64 = c->precision == CB_F64;
+  a.llr_out = f64 ? (double*)l->d_llr : nullptr;
+  a.llr_out_f32 = f64 ? nullptr : (float*)l->d_llr;
   a.payload_out = (uint32_t*)l->d_payload;
   a.raw_errors_out = (uint32_t*)l->d_raw;
   LINK_CUDA(l, cbk::launch_link_gen(a, s));
-  if (cb_status st = decode_impl<double>(c, (const double*)l->d_llr, n * l->blocks, (double*)l->d_post,
-                                         (int32_t*)l->d_iters, s))
+  if (cb_status st = f64 ? decode_impl<double>(c, (const double*)l->d_llr, n * l->blocks, (double*)l->d_post,
+                                               (int32_t*)l->d_iters, s)
+                          : decode_impl<float>(c, (const float*)l->d_llr, n * l->blocks, (float*)l->d_post,
+                                               (int32_t*)l->d_iters, s))
     return kfail(l, st, c->err);
   if (count) {
     cbk::LinkCountArgs ca;
@@ -429,7 +433,8 @@ cb_status link_run_device(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_
     ca.n = c->host.n;
     ca.blocks = l->blocks;
     ca.info_pos = c->d_enc;
-    ca.post = (const double*)l->d_post;
+    ca.post = f64 ? (const double*)l->d_post : nullptr;
+    ca.post_f32 = f64 ? nullptr : (const float*)l->d_post;
     ca.iters = (const int32_t*)l->d_iters;
     ca.payload = (const uint32_t*)l->d_payload;
     ca.raw_errors = (const uint32_t*)l->d_raw;
@@ -650,7 +655,6 @@ cb_status cb_link_create(cb_ldpc* code, int32_t blocks, int32_t modulation_order
   if (!out) return kfail(nullptr, CB_ERR_CONFIG, "null output pointer");
   *out = nullptr;
   if (!code) return kfail(nullptr, CB_ERR_CONFIG, "null code");
-  if (code->precision != CB_F64) return kfail(nullptr, CB_ERR_CONFIG, "the link runs in f64: create the code with CB_F64");
   if (code->enc.kind != cbh::kEncoderSums)
     return kfail(nullptr, CB_ERR_CONFIG, "the link needs the from_rows encoder: cb_ldpc_set_encoder(CB_ENC_SUMS)");
   if (blocks < 1) return kfail(nullptr, CB_ERR_CONFIG, "blocks must be >= 1");
@@ -792,13 +796,20 @@ cb_status cb_link_generate(cb_link* l, uint64_t seed, uint64_t name_hash, uint64
                                        l->code->stream))
       return st;
     cudaStream_t s = l->code->stream;
-    if (llr) LINK_CUDA(l, cudaMemcpyAsync(llr + f0 * nb, l->d_llr, cnt * nb * 8, cudaMemcpyDeviceToHost, s));
+    std::vector<float> l32;
+    if (llr && l->code->precision == CB_F64)
+      LINK_CUDA(l, cudaMemcpyAsync(llr + f0 * nb, l->d_llr, cnt * nb * 8, cudaMemcpyDeviceToHost, s));
+    if (llr && l->code->precision != CB_F64) {
+      l32.resize((size_t)cnt * nb);
+      LINK_CUDA(l, cudaMemcpyAsync(l32.data(), l->d_llr, l32.size() * 4, cudaMemcpyDeviceToHost, s));
+    }
     if (raw_errors) LINK_CUDA(l, cudaMemcpyAsync(raw_errors + f0, l->d_raw, cnt * 4, cudaMemcpyDeviceToHost, s));
     if (payload) {
       words.resize((size_t)cnt * l->blocks * wk);
       LINK_CUDA(l, cudaMemcpyAsync(words.data(), l->d_payload, words.size() * 4, cudaMemcpyDeviceToHost, s));
     }
     LINK_CUDA(l, cudaStreamSynchronize(s));
+    for (size_t i = 0; i < l32.size(); i++) llr[f0 * nb + i] = (double)l32[i];
     if (payload)
       for (int64_t t = 0; t < cnt; t++)
         for (int b = 0; b < l->blocks; b++)

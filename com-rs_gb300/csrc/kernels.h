@@ -253,14 +253,16 @@ struct LinkGenArgs {
   const int32_t* lookup;     // [m]: the label of cell (row, col) at row * side + col
   uint64_t seed, name_hash, cond, first_trial;
   int64_t n_trials;
-  double* llr_out;           // [n_trials][n x blocks], deinterleaved
+  double* llr_out;           // [n_trials][n x blocks], deinterleaved (f64 decoder)
+  float* llr_out_f32;        // the same rounded to f32 (f32 decoder); one of the two is null
   uint32_t* payload_out;     // [n_trials][blocks][ceil(k/32)]
   uint32_t* raw_errors_out;  // [n_trials]
 };
 struct LinkCountArgs {
   int32_t k, n, blocks;
   const int32_t* info_pos;
-  const double* post;        // [n_trials x blocks][n]
+  const double* post;        // [n_trials x blocks][n] (f64 decoder)
+  const float* post_f32;     // the same from an f32 decoder; one of the two is null
   const int32_t* iters;      // [n_trials x blocks]
   const uint32_t* payload;   // [n_trials][blocks][ceil(k/32)]
   const uint32_t* raw_errors;

@@ -9,7 +9,8 @@
 //               symbol order (blocks/channel.rs:141-156, blocks/frame.rs:250-259);
 //   demap       exact or max-log LLRs (blocks/coding/map.rs:55-77);
 //   fec_decode  the first n x blocks LLRs deinterleaved: decoder input perm[t] takes LLR t
-//               (fec.rs:88-102); the blocks then go through the generic decoder.
+//               (fec.rs:88-102); the blocks then go through the generic decoder.  With
+//               an f32 decoder the f64 LLRs are rounded once to f32.
 // The uncoded bit errors of the metric ber are counted here: the samples scaled by
 // sqrt(energy(x) / energy(y)) and decided by the grid slicer of the square QAM
 // (crates/com-spec/src/metrics.rs:254-284, :374-383, crates/com-math/src/nearest.rs),
@@ -121,7 +122,8 @@ __global__ void __launch_bounds__(NT) link_gen_kernel(const __grid_constant__ Li
   const double sigma2 = s_sigma2;
   // ---- noise and LLRs, symbol chunk [tid * spc, (tid + 1) * spc); the LLR of stream bit
   // t goes to decoder input perm[t]
-  double* llr = a.llr_out + trial * (int64_t)nb;
+  double* llr = a.llr_out ? a.llr_out + trial * (int64_t)nb : nullptr;
+  float* llr32 = a.llr_out_f32 ? a.llr_out_f32 + trial * (int64_t)nb : nullptr;
   {
     const int s0 = tid * a.syms_per_chunk, s1 = min(s0 + a.syms_per_chunk, n_sym);
     if (s0 < s1) {
@@ -139,7 +141,9 @@ __global__ void __launch_bounds__(NT) link_gen_kernel(const __grid_constant__ Li
         const int t0 = s * a.mbits;
         demap_f64(pts, a.m, a.mbits, a.log_m, a.exact != 0, yre, yim, sigma2, nb - t0, [&](int o, double v) {
           const int t = t0 + o;
-          llr[a.perm ? a.perm[t] : t] = v;
+          const int pos = a.perm ? a.perm[t] : t;
+          if (llr32) llr32[pos] = (float)v;
+          else llr[pos] = v;
         });
       }
     }
@@ -180,11 +184,12 @@ __global__ void __launch_bounds__(NT) link_count_kernel(const __grid_constant__ 
   for (int blk = 0; blk < a.blocks; blk++) {
     if (threadIdx.x == 0) s_blk = 0;
     __syncthreads();
-    const double* post = a.post + (trial * a.blocks + blk) * (int64_t)a.n;
+    const int64_t base = (trial * a.blocks + blk) * (int64_t)a.n;
     const uint32_t* u = a.payload + trial * (int64_t)(a.blocks * wk) + blk * wk;
     unsigned int e = 0;
     for (int i = threadIdx.x; i < a.k; i += NT) {
-      const unsigned dec = post[a.info_pos[i]] < 0.0 ? 1u : 0u;
+      const int v = a.info_pos[i];
+      const unsigned dec = (a.post_f32 ? a.post_f32[base + v] < 0.0f : a.post[base + v] < 0.0) ? 1u : 0u;
       e += dec ^ ((u[i >> 5] >> (i & 31)) & 1u);
     }
     if (e) atomicAdd(&s_blk, e);

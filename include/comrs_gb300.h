@@ -286,9 +286,10 @@ cb_status cb_ldpc_peg(int32_t n, int32_t k, int32_t var_degree, uint64_t seed, i
  *   fec_decode (fec.rs:88-102): deinterleave, decode every block with the code's decoder.
  * Trial t of condition c draws from stream(seed, name, c, t).  Per trial the counts of
  * the metrics (crates/com-spec/src/metrics.rs:254-351): ber (uncoded decisions of the
- * power-scaled samples by the grid slicer), coded_ber, bler.  The code object must be
- * f64 with the CB_ENC_SUMS encoder, and outlive the link; both are used under their
- * locks. */
+ * power-scaled samples by the grid slicer), coded_ber, bler.  The code object must have
+ * the CB_ENC_SUMS encoder and outlive the link; both are used under their locks.  The
+ * LLRs are computed in f64; a CB_F32 code decodes them rounded once to f32 (the
+ * reference decodes in f64: a CB_F64 code is the parity configuration). */
 typedef struct {
   uint32_t raw_bit_errors;   /* ber: errors of the n_sym log2 M sent bits */
   uint32_t coded_bit_errors; /* coded_ber: errors of the k x blocks payload bits */

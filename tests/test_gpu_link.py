@@ -70,6 +70,32 @@ def test_the_specification_settings_agree_with_the_oracle(cb, O):
     assert same >= 0.98 * total
 
 
+def test_f32_decoder_link_equals_the_oracle_on_rounded_llrs(cb, O):
+    # an f32 code: the f64 LLRs rounded once to f32, decoded in f32; the counts equal the
+    # oracle's f32 decoder (min-sum, bit-exact) on the same rounded LLRs
+    rows = cb.ldpc.peg_rows(1024, 512)
+    code = cb.Ldpc(1024, rows, rule="normalized_min_sum", alpha=0.75, max_iterations=20, precision="f32")
+    link = cb.Link(code, 8, 16, True, 0, "max_log")
+    link64 = cb.Link(cb.Ldpc(1024, rows, rule="normalized_min_sum", alpha=0.75, max_iterations=20), 8, 16, True, 0,
+                     "max_log")
+    ref = O.Code(rows=rows, n=1024)
+    ref.set_decoder(O.RULE_NMS, 0.75, True, 20)
+    info = code.info_positions()
+    for cond, ebn0 in enumerate((3.5, 4.5)):
+        llr32, pay, raw = link.generate(6, NAME, cond, 0, 32, ebn0)
+        llr64, pay64, raw64 = link64.generate(6, NAME, cond, 0, 32, ebn0)
+        assert np.array_equal(pay, pay64) and np.array_equal(raw, raw64)
+        assert np.array_equal(llr32, llr64.astype(np.float32).astype(np.float64))
+        post, its = ref.decode_llr_many(llr32.reshape(-1, 1024).astype(np.float32), "f32")
+        dec = (post[:, info] < 0).astype(np.uint8)
+        err = (dec != pay.reshape(-1, 512)).sum(axis=1).reshape(32, 8)
+        rec = link.run_trials(6, NAME, cond, 0, 32, ebn0)
+        assert np.array_equal(rec["coded_bit_errors"], err.sum(axis=1))
+        assert np.array_equal(rec["block_errors"], (err > 0).sum(axis=1))
+        assert np.array_equal(rec["iterations"], its.reshape(32, 8).sum(axis=1))
+        assert np.array_equal(rec["raw_bit_errors"], raw)
+
+
 def _spec(**over):
     s = copy.deepcopy(BICM_LDPC)
     s.update(over)
