@@ -48,10 +48,9 @@ __device__ __forceinline__ T clamp_t(T x, T lo, T hi) {
   return x < lo ? lo : (x > hi ? hi : x);
 }
 
-// One check node.  in(i): the incoming message of edge i (post - c2v, recomputed on
-// each pass, always to the same value).  Layered: the outputs go to msg (replacing the
-// old messages after they are read) and to post; flooding: to out only.  aux holds the
-// prefix products of the sum-product rule.
+// One check node.  The incoming message of edge i is post - c2v.  Layered: the outputs
+// go to msg (replacing the old messages after they are read) and to post; flooding: to
+// out only.  aux holds the prefix products of the sum-product rule.
 // Edge k of a row: its message slot and its variable, in the row-major layout (slot
 // e0 + k) or the transposed one (slot k m + pos, consecutive for consecutive threads).
 struct EdgeSlots {
@@ -67,26 +66,30 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, int pos, 
   const int d = c.row_start[row + 1] - c.row_start[row];
   const EdgeSlots es = c.tvars ? EdgeSlots{c.tvars, pos, c.m} : EdgeSlots{c.vars, c.row_start[row], 1};
   if (RULE == cbd::RULE_SUM_PRODUCT) {
-    // the product of the other tanh(L/2) by prefix and suffix products
+    // the product of the other tanh(L/2) by prefix and suffix products.  The first pass
+    // keeps each edge's tanh(l/2) in the edge's message slot, whose old message it no
+    // longer needs, so that the second pass does not compute it again; layered, l goes to
+    // the variable's posterior (no other row of the level touches that variable).
     T prefix = (T)1;
     for (int k = 0; k < d; k++) {
-      const int e = es.slot(k);
-      const T l = sub_rn(post[es.var(k)], msg[e]);
+      const int e = es.slot(k), v = es.var(k);
+      const T l = sub_rn(post[v], msg[e]);
       const T t = tanh_t(mul_rn(l, (T)0.5));
       aux[e] = prefix;
       prefix = mul_rn(prefix, t);
+      msg[e] = t;
+      if (LAYERED) post[v] = l;
     }
     T suffix = (T)1;
     for (int k = d - 1; k >= 0; k--) {
       const int e = es.slot(k), v = es.var(k);
-      const T l = sub_rn(post[v], msg[e]);
-      const T t = tanh_t(mul_rn(l, (T)0.5));
+      const T t = msg[e];
       const T p = mul_rn(aux[e], suffix);
       suffix = mul_rn(suffix, t);
       const T o = mul_rn((T)2, atanh_t(clamp_t(p, -tanh_bound<T>(), tanh_bound<T>())));
       if (LAYERED) {
         msg[e] = o;
-        post[v] = add_rn(l, o);
+        post[v] = add_rn(post[v], o);
       } else {
         out[e] = o;
       }
