@@ -445,15 +445,41 @@ def _value(v, cond):
     return v
 
 
-def run_spec(spec, device=0, on_batch=None):
+def _parse(spec):
+    if isinstance(spec, str):
+        spec = load_yaml(open(spec).read() if os.path.exists(spec) else spec)
+    return spec
+
+
+def run_spec(spec, device=0, on_batch=None, rank=0, world=1, all_reduce=None):
     """The campaign of a specification (a mapping, a YAML text or a file name): one
     ConditionResult per condition in grid order, with the ErrorRate of every reported
     metric (``ber``, ``coded_ber``, ``bler``) and the decoder's iterations per block;
-    conditions that ``skip_below`` skips come back with status ``skipped``."""
+    conditions that ``skip_below`` skips come back with status ``skipped``.
+
+    Several processes (one GPU each) run one campaign together as :func:`run` does:
+    process ``rank`` of ``world`` runs its contiguous share of every batch, and
+    ``all_reduce`` (summing an int64 vector over the processes) merges the counts before
+    the stop rule; the result equals the one-process campaign."""
     from . import fnv1a64  # noqa: F401  (the library must load before any work)
 
-    if isinstance(spec, str):
-        spec = load_yaml(open(spec).read() if os.path.exists(spec) else spec)
+    spec = _parse(spec)
+    link, s = build_link(spec, device)
+    try:
+        return run_spec_with(link, spec, on_batch, rank, world, all_reduce)
+    finally:
+        link.close()
+
+
+def run_spec_with(link, spec, on_batch=None, rank=0, world=1, all_reduce=None):
+    """The campaign of `spec` on `link`: anything with run_trials(seed, name, condition,
+    first_trial, n_trials, ebn0_db) returning LINK_DTYPE records and the attributes
+    sent_bits, payload_bits and blocks (:class:`Link`, or a stand-in computing the same
+    trials elsewhere)."""
+    spec = _parse(spec)
+    if world > 1 and all_reduce is None:
+        raise ValueError("a multi-process campaign needs all_reduce")
+    s = _link_settings(spec["link"])
     name, seed, batch = spec["name"], int(spec.get("seed", 0)), max(1, int(spec.get("batch", 32)))
     grid = Grid()
     for k, v in (spec.get("grid") or {}).items():
@@ -466,7 +492,6 @@ def run_spec(spec, device=0, on_batch=None):
     if not stop.is_bounded():
         raise ValueError("the stopping rule can run forever: add max_trials")
     skip = ((spec.get("callbacks") or {}).get("skip_below"))
-    link, s = build_link(spec, device)
     done, results = [], []
     for index, cond in enumerate(grid.conditions()):
         others = sorted((k, v) for k, v in cond.items() if not skip or k != skip["along"])
@@ -480,15 +505,22 @@ def run_spec(spec, device=0, on_batch=None):
         trials, limit = 0, stop.trial_limit()
         while True:
             end = trials + batch if limit is None else max(min(trials + batch, limit), trials + 1)
-            r = link.run_trials(seed, name, index, trials, end - trials, ebn0)
-            n = len(r)
+            n = end - trials
+            lo, hi = trials + n * rank // world, trials + n * (rank + 1) // world
+            counts = np.zeros(4, np.int64)
+            if hi > lo:
+                r = link.run_trials(seed, name, index, lo, hi - lo, ebn0)
+                counts[:] = (r["raw_bit_errors"].sum(dtype="u8"), r["coded_bit_errors"].sum(dtype="u8"),
+                             r["block_errors"].sum(dtype="u8"), r["iterations"].sum(dtype="u8"))
+            if world > 1:
+                counts = all_reduce(counts)
             if "ber" in rec:
-                rec["ber"].add(int(r["raw_bit_errors"].sum(dtype="u8")), link.sent_bits * n)
+                rec["ber"].add(int(counts[0]), link.sent_bits * n)
             if "coded_ber" in rec:
-                rec["coded_ber"].add(int(r["coded_bit_errors"].sum(dtype="u8")), link.payload_bits * n)
+                rec["coded_ber"].add(int(counts[1]), link.payload_bits * n)
             if "bler" in rec:
-                rec["bler"].add(int(r["block_errors"].sum(dtype="u8")), link.blocks * n)
-            its.add_many(n * link.blocks, int(r["iterations"].sum(dtype="u8")))
+                rec["bler"].add(int(counts[2]), link.blocks * n)
+            its.add_many(n * link.blocks, int(counts[3]))
             trials = end
             if on_batch:
                 on_batch(index, trials, rec)
@@ -500,5 +532,4 @@ def run_spec(spec, device=0, on_batch=None):
             e = rec.get(skip["metric"].lower())
             if trials > 0 and e is not None and e.rate() < float(skip["threshold"]) and others not in done:
                 done.append(others)
-    link.close()
     return results

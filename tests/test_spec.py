@@ -134,3 +134,101 @@ def test_link_without_a_gpu_fails_loudly(cb):
     with pytest.raises(cb.ComrsError) as e:
         link.run_trials(1, "x", 0, 0, 4, 3.0)
     assert e.value.status == -6
+
+
+class OracleLink:
+    """The run_trials surface of the GPU Link, computed by the oracle (CPU)."""
+
+    def __init__(self, O, cb, n, k, blocks, m, il_seed, exact, rule, alpha, iters):
+        self.O = O
+        self.code = O.Code(rows=cb.ldpc.peg_rows(n, k), n=n)
+        self.code.set_decoder(rule, alpha, True, iters)
+        self.code.set_demapper(exact)
+        self.blocks, self.m, self.il_seed = blocks, m, il_seed
+        self.sent_bits = n * blocks + (-(n * blocks)) % int(np.log2(m))
+        self.payload_bits = k * blocks
+
+    def run_trials(self, seed, name, cond, first, n, ebn0):
+        out, _, _ = self.code.link_trials(self.blocks, self.il_seed, self.m, seed, self.O.fnv1a64(name), cond, first,
+                                          n, ebn0, self.O.NOISE_CR, 1)
+        rec = np.zeros(n, [("raw_bit_errors", "<u4"), ("coded_bit_errors", "<u4"), ("block_errors", "<u4"),
+                           ("iterations", "<u4")])
+        rec["raw_bit_errors"], rec["coded_bit_errors"] = out[:, 0], out[:, 2]
+        rec["block_errors"], rec["iterations"] = out[:, 4], out[:, 6]
+        return rec
+
+
+SMALL = {"name": "bicm_small", "seed": 3, "batch": 6, "grid": {"ebn0_db": [2.0, 5.0, 7.0, 9.0]},
+         "link": [{"type": "fec_encode", "code": {"type": "ldpc", "n": 96, "k": 48, "rule": "normalized_min_sum",
+                                                  "alpha": 0.75, "iterations": 20}, "blocks": 3, "interleave": True},
+                  {"type": "map", "constellation": "16-QAM"}, {"type": "awgn_ebn0", "ebn0_db": "$ebn0_db"},
+                  {"type": "demap", "max_log": True},
+                  {"type": "fec_decode", "code": {"type": "ldpc", "n": 96, "k": 48, "rule": "normalized_min_sum",
+                                                  "alpha": 0.75, "iterations": 20}, "interleave": True}],
+         "stop": {"min_errors": {"bler": 12}, "min_trials": 6, "max_trials": 40},
+         "callbacks": {"skip_below": {"metric": "bler", "threshold": 0.05, "along": "ebn0_db"}}}
+
+
+def _small_link(O, cb):
+    return OracleLink(O, cb, 96, 48, 3, 16, 0, False, O.RULE_NMS, 0.75, 20)
+
+
+def _summary(res):
+    return [(r.status, r.trials) + tuple((e.errors, e.total) for k, e in sorted(r.record.items()) if k != "iterations")
+            + ((r.record["iterations"].total,) if "iterations" in r.record else ()) for r in res]
+
+
+def _spec_rank(rank, world, port, out):
+    import sys
+
+    from conftest import ROOT
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import torch.distributed as dist
+
+    import oracle as O
+    from conftest import load_package
+
+    cb = load_package()
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+
+    def all_reduce(v):
+        import torch
+
+        t = torch.from_numpy(np.asarray(v, np.int64).copy())
+        dist.all_reduce(t)
+        return t.numpy()
+
+    spec = __import__("importlib").import_module("com-rs_gb300.spec")
+    out[rank] = _summary(spec.run_spec_with(_small_link(O, cb), SMALL, rank=rank, world=world, all_reduce=all_reduce))
+    dist.destroy_process_group()
+
+
+def test_spec_campaign_semantics_and_two_processes(cb, O):
+    # run_spec's loop on the oracle's trials: batches of 6, (min_errors and min_trials) or
+    # max_trials, skip_below; two gloo processes give the one-process result
+    import socket
+
+    import torch.multiprocessing as mp
+
+    spec = __import__("importlib").import_module("com-rs_gb300.spec")
+    one = spec.run_spec_with(_small_link(O, cb), SMALL)
+    assert [r.status for r in one][:1] == ["completed"]
+    for r in one:
+        if r.status == "completed":
+            b = r.record["bler"]
+            assert r.trials == 40 or (b.errors >= 12 and r.trials >= 6)
+            assert r.trials % 6 == 0 or r.trials == 40
+    assert [r.status for r in one] == ["completed"] * 3 + ["skipped"]  # the floor is reached at 7 dB
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    out = ctx.Manager().dict()
+    procs = [ctx.Process(target=_spec_rank, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    assert out[0] == out[1] == _summary(one)
