@@ -41,6 +41,8 @@ struct cb_ldpc {
   bool msgs_in_smem = false;
   bool post_in_smem = true;
   bool warp_rows = false;
+  bool regs = false;     // layered sum-product rows in registers
+  bool has_aux = true;   // a second message buffer
   void* kernel = nullptr;
   cudaStream_t stream = nullptr;
   void* d_llr = nullptr;
@@ -116,8 +118,13 @@ cb_status ensure_device(cb_ldpc* c) {
   // the launch shape decides the message layout: a thread per row with messages in
   // global memory takes the transposed one
   c->warp_rows = c->layered && h.max_level_rows <= 8 && h.max_row_degree <= 128;
+  // rows of few edges keep the sum-product's tanh values and prefix products in registers;
+  // a second message buffer is then needed by the flooding schedule, or by the
+  // sum-product rule on longer rows (one thread a row)
+  c->regs = c->layered && c->rule == CB_RULE_SUM_PRODUCT && !c->warp_rows && h.max_row_degree <= cbk::kRegRowDegree;
+  c->has_aux = !c->layered || (c->rule == CB_RULE_SUM_PRODUCT && !c->warp_rows && !c->regs);
   const size_t post_bytes = (size_t)h.n * elem(c);
-  const size_t msg_bytes_rm = (size_t)2 * h.edges * elem(c);
+  const size_t msg_bytes_rm = (size_t)(c->has_aux ? 2 : 1) * h.edges * elem(c);
   c->msgs_in_smem = post_bytes + msg_bytes_rm <= kSmemMsgBudget;
   c->post_in_smem = post_bytes <= kSmemPostBudget;
   const bool transposed = !c->msgs_in_smem && !c->warp_rows;
@@ -173,11 +180,11 @@ cb_status ensure_device(cb_ldpc* c) {
     const int want = c->layered ? h.max_level_rows : std::max(h.m, h.n) / 4;
     c->threads = std::min(512, std::max(64, (want + 31) / 32 * 32));
   }
-  const size_t msg_bytes = (size_t)2 * d.slots * elem(c);
+  const size_t msg_bytes = (size_t)(c->has_aux ? 2 : 1) * d.slots * elem(c);
   c->smem = c->msgs_in_smem ? ((post_bytes + msg_bytes + 15) & ~(size_t)15)
                             : (c->post_in_smem ? ((post_bytes + 15) & ~(size_t)15) : 0);
   const size_t slot_bytes = msg_bytes + (c->post_in_smem ? 0 : post_bytes);
-  c->kernel = cbk::sparse_kernel_ptr(c->precision == CB_F64 ? 0 : 1, c->rule, c->layered != 0);
+  c->kernel = cbk::sparse_kernel_ptr(c->precision == CB_F64 ? 0 : 1, c->rule, c->layered != 0, c->regs);
   LDPC_CUDA(c, cudaFuncSetAttribute(c->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
   int per_sm = 0, sms = 0;
   LDPC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c->kernel, c->threads, c->smem));
@@ -203,6 +210,7 @@ cb_status decode_impl(cb_ldpc* c, const T* llr, int64_t n, T* post, int32_t* ite
   a.msgs_in_smem = c->msgs_in_smem ? 1 : 0;
   a.post_in_smem = c->post_in_smem ? 1 : 0;
   a.warp_rows = c->warp_rows ? 1 : 0;
+  a.has_aux = c->has_aux ? 1 : 0;
   a.llr = llr;
   a.n_frames = n;
   a.post_out = post;

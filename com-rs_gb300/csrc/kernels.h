@@ -195,15 +195,19 @@ struct SparseArgs {
   int32_t post_in_smem;  // 1: the posteriors live in shared memory, else in `slots` too
   int32_t msgs_in_smem;  // 1: the edge messages live in shared memory, else in `slots`
   int32_t warp_rows;     // layered: one warp per row (levels of few rows), else one thread
+  int32_t has_aux;       // 1: a second buffer of `slots` (flooding's new messages, or the
+                         // sum-product rule's prefix products when they are not in registers)
   const T* llr;          // [n_frames][n]
   int64_t n_frames;
   T* post_out;           // [n_frames][n] (nullable)
   int32_t* iters_out;    // [n_frames] (nullable)
-  T* slots;              // [grid][2 edges (+ n when !post_in_smem)] when !msgs_in_smem
+  T* slots;              // [grid][(1 + has_aux) slots (+ n when !post_in_smem)] when !msgs_in_smem
   unsigned long long* work_counter;
 };
-// the kernel of a precision (0: f64, 1: f32), rule and schedule
-void* sparse_kernel_ptr(int precision, int rule, bool layered);
+// the kernel of a precision (0: f64, 1: f32), rule and schedule; regs: the layered
+// sum-product rows in registers, for codes whose rows have at most kRegRowDegree edges
+constexpr int kRegRowDegree = 8;
+void* sparse_kernel_ptr(int precision, int rule, bool layered, bool regs);
 cudaError_t launch_sparse(void* kernel, const void* args, int grid, int threads, size_t smem, cudaStream_t stream);
 
 // ---- systematic encoders of generic codes (sparse_encode.cu)

@@ -127,6 +127,37 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, int pos, 
   }
 }
 
+// The layered sum-product row of check_row with its tanh values and prefix products in
+// registers (rows of at most MAXD edges): the same operations in the same order, without
+// the prefix buffer.
+template <typename T, int MAXD>
+__device__ __forceinline__ void check_row_spa_regs(const SparseDev& c, int row, int pos, T* post, T* msg) {
+  const int d = c.row_start[row + 1] - c.row_start[row];
+  const EdgeSlots es = c.tvars ? EdgeSlots{c.tvars, pos, c.m} : EdgeSlots{c.vars, c.row_start[row], 1};
+  T l[MAXD], t[MAXD], pre[MAXD];
+  T prefix = (T)1;
+#pragma unroll
+  for (int k = 0; k < MAXD; k++) {
+    if (k < d) {
+      l[k] = sub_rn(post[es.var(k)], msg[es.slot(k)]);
+      t[k] = tanh_t(mul_rn(l[k], (T)0.5));
+      pre[k] = prefix;
+      prefix = mul_rn(prefix, t[k]);
+    }
+  }
+  T suffix = (T)1;
+#pragma unroll
+  for (int k = MAXD - 1; k >= 0; k--) {
+    if (k < d) {
+      const T p = mul_rn(pre[k], suffix);
+      suffix = mul_rn(suffix, t[k]);
+      const T o = mul_rn((T)2, atanh_t(clamp_t(p, -tanh_bound<T>(), tanh_bound<T>())));
+      msg[es.slot(k)] = o;
+      post[es.var(k)] = add_rn(l[k], o);
+    }
+  }
+}
+
 // One check node by a warp (layered schedule, levels of few rows): lane i takes edges
 // i, i + 32, ... of the row.  Min-sum: a warp reduction of (minimum, first index of the
 // minimum, second minimum) and of the sign parity gives the sequential loop's values
@@ -244,24 +275,27 @@ __device__ __forceinline__ bool some_row_fails(const SparseDev& c, const T* post
   return __syncthreads_or(bad) != 0;
 }
 
-template <typename T, int RULE, bool LAYERED>
+// REGS: the layered sum-product rows keep their tanh values and prefix products in
+// registers (check_row_spa_regs; every row of at most kRegRowDegree edges)
+template <typename T, int RULE, bool LAYERED, bool REGS>
 __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ SparseArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SparseDev& c = a.code;
   const int tid = threadIdx.x, nt = blockDim.x;
+  // the messages, then (when the schedule needs one) the second buffer: the flooding
+  // schedule's new messages or the sum-product rule's prefix products
+  const size_t bufs = (size_t)(a.has_aux ? 2 : 1) * c.slots;
   T* post;
   T* msg;
-  T* aux;
   if (a.msgs_in_smem) {
     post = reinterpret_cast<T*>(smem);
     msg = post + c.n;
-    aux = msg + c.slots;
   } else {
-    const size_t per = (size_t)2 * c.slots + (a.post_in_smem ? 0 : (size_t)c.n);
+    const size_t per = bufs + (a.post_in_smem ? 0 : (size_t)c.n);
     msg = a.slots + (size_t)blockIdx.x * per;
-    aux = msg + c.slots;
-    post = a.post_in_smem ? reinterpret_cast<T*>(smem) : aux + c.slots;
+    post = a.post_in_smem ? reinterpret_cast<T*>(smem) : msg + bufs;
   }
+  T* aux = a.has_aux ? msg + c.slots : nullptr;
   const T alpha = (T)a.alpha;
   __shared__ long long s_cw;
   for (;;) {
@@ -273,7 +307,7 @@ __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ Spa
     for (int v = tid; v < c.n; v += nt) post[v] = llr[v];
     for (int e = tid; e < c.slots; e += nt) {
       msg[e] = (T)0;
-      aux[e] = (T)0;
+      if (aux) aux[e] = (T)0;
     }
     __syncthreads();
     int it = 0;
@@ -292,8 +326,10 @@ __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ Spa
         } else if (LAYERED) {
           for (int L = 0; L < c.levels; L++) {
             const int r0 = c.level_start[L], r1 = c.level_start[L + 1];
-            for (int i = r0 + tid; i < r1; i += nt)
-              check_row<T, RULE, true>(c, c.level_rows[i], i, post, msg, nullptr, aux, alpha);
+            for (int i = r0 + tid; i < r1; i += nt) {
+              if constexpr (REGS) check_row_spa_regs<T, kRegRowDegree>(c, c.level_rows[i], i, post, msg);
+              else check_row<T, RULE, true>(c, c.level_rows[i], i, post, msg, nullptr, aux, alpha);
+            }
             __syncthreads();
           }
         } else {
@@ -324,21 +360,23 @@ __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ Spa
 }
 
 template <typename T>
-void* sparse_kernel_for(int rule, bool layered) {
+void* sparse_kernel_for(int rule, bool layered, bool regs) {
   if (layered) {
-    if (rule == cbd::RULE_SUM_PRODUCT) return (void*)sparse_kernel<T, cbd::RULE_SUM_PRODUCT, true>;
-    if (rule == cbd::RULE_NMS) return (void*)sparse_kernel<T, cbd::RULE_NMS, true>;
-    return (void*)sparse_kernel<T, cbd::RULE_OMS, true>;
+    if (rule == cbd::RULE_SUM_PRODUCT)
+      return regs ? (void*)sparse_kernel<T, cbd::RULE_SUM_PRODUCT, true, true>
+                  : (void*)sparse_kernel<T, cbd::RULE_SUM_PRODUCT, true, false>;
+    if (rule == cbd::RULE_NMS) return (void*)sparse_kernel<T, cbd::RULE_NMS, true, false>;
+    return (void*)sparse_kernel<T, cbd::RULE_OMS, true, false>;
   }
-  if (rule == cbd::RULE_SUM_PRODUCT) return (void*)sparse_kernel<T, cbd::RULE_SUM_PRODUCT, false>;
-  if (rule == cbd::RULE_NMS) return (void*)sparse_kernel<T, cbd::RULE_NMS, false>;
-  return (void*)sparse_kernel<T, cbd::RULE_OMS, false>;
+  if (rule == cbd::RULE_SUM_PRODUCT) return (void*)sparse_kernel<T, cbd::RULE_SUM_PRODUCT, false, false>;
+  if (rule == cbd::RULE_NMS) return (void*)sparse_kernel<T, cbd::RULE_NMS, false, false>;
+  return (void*)sparse_kernel<T, cbd::RULE_OMS, false, false>;
 }
 
 }  // namespace
 
-void* sparse_kernel_ptr(int precision, int rule, bool layered) {
-  return precision == 0 ? sparse_kernel_for<double>(rule, layered) : sparse_kernel_for<float>(rule, layered);
+void* sparse_kernel_ptr(int precision, int rule, bool layered, bool regs) {
+  return precision == 0 ? sparse_kernel_for<double>(rule, layered, regs) : sparse_kernel_for<float>(rule, layered, regs);
 }
 
 cudaError_t launch_sparse(void* kernel, const void* args, int grid, int threads, size_t smem, cudaStream_t s) {
