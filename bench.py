@@ -492,6 +492,36 @@ def run_spec_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def run_spec_profile_case(args):
+    """The small case of the spec link for ncu: `trials` trials generated once at 2.5 dB,
+    their codewords then decoded three times by the f64 and three times by the f32
+    generic decoder."""
+    import torch
+
+    cb = importlib.import_module("com-rs_gb300")
+    L = cb.lib()
+    T = args.trials
+    sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = {}
+    for prec in ("f64", "f32"):
+        code = cb.Ldpc.peg(SPEC_N, SPEC_K, rule="sum_product", max_iterations=50, precision=prec)
+        link = cb.Link(code, SPEC_BLOCKS, SPEC_M, True, 0, "exact")
+        llr_h, _, _ = link.generate(SPEC_SEED, SPEC_NAME, 0, 0, T, SPEC_GRID[0])
+        llr = torch.from_numpy(llr_h if prec == "f64" else llr_h.astype(np.float32)).cuda()
+        post = torch.empty_like(llr)
+        iters = torch.empty(T * SPEC_BLOCKS, dtype=torch.int32, device="cuda")
+        st = 0
+        for _ in range(3):
+            st |= L.cb_ldpc_decode_device(code._h, C.c_void_p(llr.data_ptr()), T * SPEC_BLOCKS,
+                                          C.c_void_p(post.data_ptr()), C.c_void_p(iters.data_ptr()), sp)
+        torch.cuda.synchronize()
+        if st:
+            raise cb.ComrsError(st, L.cb_ldpc_last_error(code._h).decode())
+        out[prec] = float(iters.float().mean())
+        link.close()
+    print(json.dumps({"profile_case": "spec", "trials": T, "mean_iterations": out}))
+
+
 def run_profile_case(args):
     """The small case the committed ncu summaries capture: `frames` C2 codewords generated
     once (Eb/N0 = 1 dB), then decoded three times."""
@@ -529,10 +559,14 @@ def main():
                     help="c2: the NR trial (the headline); spec: the link of specs/bicm_ldpc.yaml")
     ap.add_argument("--trials", type=int, default=2048, help="trials per step of --workload spec")
     ap.add_argument("--profile-case", action="store_true",
-                    help="generate --frames C2 codewords and decode them three times (for ncu)")
+                    help="generate --frames C2 codewords (--workload spec: --trials trials) and decode them "
+                         "three times (for ncu)")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args)
+        if args.workload == "spec":
+            run_spec_profile_case(args)
+        else:
+            run_profile_case(args)
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
