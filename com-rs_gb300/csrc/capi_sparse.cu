@@ -23,6 +23,8 @@ thread_local std::string g_ldpc_thread_error;
 // two CTAs resident per SM; and the posteriors, before they move there too
 constexpr size_t kSmemMsgBudget = 100 * 1024;
 constexpr size_t kSmemPostBudget = 200 * 1024;
+// shared memory of a CTA of several small codewords: two CTAs per SM
+constexpr size_t kGroupSmem = 100 * 1024;
 
 }  // namespace
 
@@ -43,6 +45,7 @@ struct cb_ldpc {
   bool warp_rows = false;
   bool regs = false;     // layered sum-product rows in registers
   bool has_aux = true;   // a second message buffer
+  int group = 1;         // codewords per CTA
   void* kernel = nullptr;
   cudaStream_t stream = nullptr;
   void* d_llr = nullptr;
@@ -185,6 +188,20 @@ cb_status ensure_device(cb_ldpc* c) {
                             : (c->post_in_smem ? ((post_bytes + 15) & ~(size_t)15) : 0);
   const size_t slot_bytes = msg_bytes + (c->post_in_smem ? 0 : post_bytes);
   c->kernel = cbk::sparse_kernel_ptr(c->precision == CB_F64 ? 0 : 1, c->rule, c->layered != 0, c->regs);
+  // small layered codes with one thread per row: several codewords per CTA (up to
+  // kGroupSmem of shared memory), so that the rows of a level fill the warps
+  c->group = 1;
+  if (c->layered && !c->warp_rows && c->msgs_in_smem) {
+    const size_t per = (h.n + (size_t)(c->has_aux ? 2 : 1) * h.edges) * elem(c);
+    c->group = (int)std::min<size_t>(cbk::kMaxGroup, kGroupSmem / per);
+    if (c->group >= 2) {
+      c->kernel = cbk::sparse_group_kernel_ptr(c->precision == CB_F64 ? 0 : 1, c->rule, c->regs);
+      c->smem = (c->group * per + 15) & ~(size_t)15;
+      c->threads = std::min(512, (c->group * h.max_level_rows + 31) / 32 * 32);
+    } else {
+      c->group = 1;
+    }
+  }
   LDPC_CUDA(c, cudaFuncSetAttribute(c->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
   int per_sm = 0, sms = 0;
   LDPC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c->kernel, c->threads, c->smem));
@@ -211,6 +228,7 @@ cb_status decode_impl(cb_ldpc* c, const T* llr, int64_t n, T* post, int32_t* ite
   a.post_in_smem = c->post_in_smem ? 1 : 0;
   a.warp_rows = c->warp_rows ? 1 : 0;
   a.has_aux = c->has_aux ? 1 : 0;
+  a.group = c->group;
   a.llr = llr;
   a.n_frames = n;
   a.post_out = post;
@@ -218,7 +236,7 @@ cb_status decode_impl(cb_ldpc* c, const T* llr, int64_t n, T* post, int32_t* ite
   a.slots = reinterpret_cast<T*>(c->d_slots);
   a.work_counter = c->d_counter;
   LDPC_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), s));
-  const int grid = (int)std::min<int64_t>(c->grid, n);
+  const int grid = (int)std::min<int64_t>(c->grid, (n + c->group - 1) / c->group);
   LDPC_CUDA(c, cbk::launch_sparse(c->kernel, &a, grid, c->threads, c->smem, s));
   return CB_OK;
 }

@@ -197,6 +197,7 @@ struct SparseArgs {
   int32_t warp_rows;     // layered: one warp per row (levels of few rows), else one thread
   int32_t has_aux;       // 1: a second buffer of `slots` (flooding's new messages, or the
                          // sum-product rule's prefix products when they are not in registers)
+  int32_t group;         // codewords per CTA (sparse_group_kernel; 1 for sparse_kernel)
   const T* llr;          // [n_frames][n]
   int64_t n_frames;
   T* post_out;           // [n_frames][n] (nullable)
@@ -208,6 +209,10 @@ struct SparseArgs {
 // sum-product rows in registers, for codes whose rows have at most kRegRowDegree edges
 constexpr int kRegRowDegree = 8;
 void* sparse_kernel_ptr(int precision, int rule, bool layered, bool regs);
+// the layered kernel with several codewords per CTA (small codes: messages and
+// posteriors of the group in shared memory, one thread per row)
+constexpr int kMaxGroup = 8;
+void* sparse_group_kernel_ptr(int precision, int rule, bool regs);
 cudaError_t launch_sparse(void* kernel, const void* args, int grid, int threads, size_t smem, cudaStream_t stream);
 
 // ---- systematic encoders of generic codes (sparse_encode.cu)

@@ -359,6 +359,108 @@ __global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ Spa
   }
 }
 
+// Layered decoding of small codes, a.group codewords per CTA, their posteriors and
+// messages in shared memory one codeword after the other.  The rows of a level of all the
+// group's codewords are spread over the threads, one row each, so that the warps run full
+// even when a level has few rows (every warp instruction costs the same issue and pipe
+// time whatever its active lanes).  Each codeword stops on its own syndrome: its rows
+// are skipped from then on.  Results equal sparse_kernel's.
+template <typename T>
+__device__ __forceinline__ void group_syndrome(const SparseDev& c, const T* base, size_t per, int G,
+                                               const int* check, volatile int* fail) {
+  for (int i = threadIdx.x; i < G * c.m; i += blockDim.x) {
+    const int g = i / c.m, r = i - g * c.m;
+    if (!check[g] || fail[g]) continue;
+    const T* post = base + g * per;
+    int par = 0;
+    for (int e = c.row_start[r]; e < c.row_start[r + 1]; e++) par ^= (int)(post[c.vars[e]] < (T)0);
+    if (par) fail[g] = 1;
+  }
+}
+
+template <typename T, int RULE, bool REGS>
+__global__ void __launch_bounds__(512) sparse_group_kernel(const __grid_constant__ SparseArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SparseDev& c = a.code;
+  const int tid = threadIdx.x, nt = blockDim.x, G = a.group;
+  const size_t bufs = (size_t)(a.has_aux ? 2 : 1) * c.slots;
+  const size_t per = (size_t)c.n + bufs;  // elements of one codeword: posteriors, then messages
+  T* base = reinterpret_cast<T*>(smem);
+  __shared__ long long s_cw[kMaxGroup];
+  __shared__ int s_run[kMaxGroup];   // 1 while the codeword decodes
+  __shared__ int s_fail[kMaxGroup];  // its syndrome fails
+  __shared__ int s_it[kMaxGroup];
+  const T alpha = (T)a.alpha;
+  for (;;) {
+    if (tid == 0) {
+      const unsigned long long b = atomicAdd(a.work_counter, (unsigned long long)G);
+      for (int g = 0; g < G; g++) s_cw[g] = (long long)(b + g);
+    }
+    __syncthreads();
+    if (s_cw[0] >= a.n_frames) break;
+    for (int g = 0; g < G; g++) {
+      T* post = base + g * per;
+      T* msg = post + c.n;
+      if (s_cw[g] < a.n_frames) {
+        const T* llr = a.llr + (size_t)s_cw[g] * c.n;
+        for (int v = tid; v < c.n; v += nt) post[v] = llr[v];
+      }
+      for (size_t e = tid; e < bufs; e += nt) msg[e] = (T)0;
+    }
+    if (tid < G) {
+      s_run[tid] = s_cw[tid] < a.n_frames ? 1 : 0;
+      s_fail[tid] = 0;
+    }
+    __syncthreads();
+    group_syndrome(c, base, per, G, s_run, s_fail);
+    __syncthreads();
+    int any = 0;
+    for (int g = 0; g < G; g++) any |= s_run[g] && s_fail[g];
+    __syncthreads();
+    if (tid < G) {
+      s_run[tid] = s_run[tid] && s_fail[tid];
+      s_it[tid] = s_run[tid] ? a.max_iterations : 0;
+    }
+    __syncthreads();
+    for (int iter = 1; iter <= a.max_iterations && any; iter++) {
+      for (int L = 0; L < c.levels; L++) {
+        const int r0 = c.level_start[L], rl = c.level_start[L + 1] - r0;
+        for (int i = tid; i < G * rl; i += nt) {
+          const int g = i / rl, j = i - g * rl;
+          if (!s_run[g]) continue;
+          T* post = base + g * per;
+          T* msg = post + c.n;
+          if constexpr (REGS) check_row_spa_regs<T, kRegRowDegree>(c, c.level_rows[r0 + j], r0 + j, post, msg);
+          else check_row<T, RULE, true>(c, c.level_rows[r0 + j], r0 + j, post, msg, nullptr,
+                                        a.has_aux ? msg + c.slots : nullptr, alpha);
+        }
+        __syncthreads();
+      }
+      if (tid < G) s_fail[tid] = 0;
+      __syncthreads();
+      group_syndrome(c, base, per, G, s_run, s_fail);
+      __syncthreads();
+      any = 0;
+      for (int g = 0; g < G; g++) any |= s_run[g] && s_fail[g];
+      __syncthreads();
+      if (tid < G && s_run[tid] && !s_fail[tid]) {
+        s_run[tid] = 0;
+        s_it[tid] = iter;
+      }
+      __syncthreads();
+    }
+    for (int g = 0; g < G; g++) {
+      const long long cw = s_cw[g];
+      if (cw >= a.n_frames) continue;
+      const T* post = base + g * per;
+      if (a.post_out)
+        for (int v = tid; v < c.n; v += nt) a.post_out[(size_t)cw * c.n + v] = post[v];
+      if (tid == 0 && a.iters_out) a.iters_out[cw] = s_it[g];
+    }
+    __syncthreads();
+  }
+}
+
 template <typename T>
 void* sparse_kernel_for(int rule, bool layered, bool regs) {
   if (layered) {
@@ -377,6 +479,19 @@ void* sparse_kernel_for(int rule, bool layered, bool regs) {
 
 void* sparse_kernel_ptr(int precision, int rule, bool layered, bool regs) {
   return precision == 0 ? sparse_kernel_for<double>(rule, layered, regs) : sparse_kernel_for<float>(rule, layered, regs);
+}
+
+template <typename T>
+void* sparse_group_kernel_for(int rule, bool regs) {
+  if (rule == cbd::RULE_SUM_PRODUCT)
+    return regs ? (void*)sparse_group_kernel<T, cbd::RULE_SUM_PRODUCT, true>
+                : (void*)sparse_group_kernel<T, cbd::RULE_SUM_PRODUCT, false>;
+  if (rule == cbd::RULE_NMS) return (void*)sparse_group_kernel<T, cbd::RULE_NMS, false>;
+  return (void*)sparse_group_kernel<T, cbd::RULE_OMS, false>;
+}
+
+void* sparse_group_kernel_ptr(int precision, int rule, bool regs) {
+  return precision == 0 ? sparse_group_kernel_for<double>(rule, regs) : sparse_group_kernel_for<float>(rule, regs);
 }
 
 cudaError_t launch_sparse(void* kernel, const void* args, int grid, int threads, size_t smem, cudaStream_t s) {
