@@ -403,6 +403,11 @@ cb_status link_ensure_device(cb_link* l) {
 cb_status link_run_device(cb_link* l, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first, int64_t n,
                           double ebn0_db, bool count, cudaStream_t s, cbk::LinkRecord* out_dev = nullptr) {
   cb_ldpc* c = l->code;
+  // the code's decoder or encoder may have been changed since the link was made
+  if (c->enc.kind != cbh::kEncoderSums)
+    return kfail(l, CB_ERR_CONFIG, "the link needs the from_rows encoder: cb_ldpc_set_encoder(CB_ENC_SUMS)");
+  if (cb_status st = ensure_encoder(c)) return kfail(l, st, c->err);
+  if (cb_status st = ensure_device(c)) return kfail(l, st, c->err);
   const cbh::SparseEncoder& e = c->enc;
   const int nb = c->host.n * l->blocks, wk = (e.k + 31) / 32;
   LINK_CUDA(l, grow_buf(&l->d_llr, l->llr_cap, (size_t)n * nb * 8));

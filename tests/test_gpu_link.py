@@ -133,3 +133,19 @@ def test_run_spec_of_the_specification_and_skip_below(cb):
     res = cb.run_spec(spec)
     assert [r.status for r in res] == ["completed", "skipped", "skipped"]
     assert res[0].trials == 8 and res[1].trials == 0
+
+
+def test_link_follows_the_codes_decoder(cb, O):
+    # set_decoder on the code after the link ran: the next trials use the new decoder
+    rows = cb.ldpc.peg_rows(96, 48)
+    code = cb.Ldpc(96, rows, rule="normalized_min_sum", alpha=0.75, max_iterations=20)
+    link = cb.Link(code, 4, 16, True, 1, "max_log")
+    link.run_trials(6, NAME, 0, 0, 8, 4.0)
+    code.set_decoder("offset_min_sum", alpha=0.15, layered=False, max_iterations=20)
+    rec = link.run_trials(6, NAME, 0, 0, 32, 4.0)
+    ref = O.Code(rows=rows, n=96)
+    ref.set_decoder(O.RULE_OMS, 0.15, False, 20)
+    ref.set_demapper(False)
+    out, _, _ = ref.link_trials(4, 1, 16, 6, O.fnv1a64(NAME), 0, 0, 32, 4.0)
+    assert np.array_equal(rec["coded_bit_errors"], out[:, 2]) and np.array_equal(rec["iterations"], out[:, 6])
+    assert np.array_equal(rec["raw_bit_errors"], out[:, 0])
