@@ -22,15 +22,65 @@ __device__ __forceinline__ void complex_gaussian_f64(cbd::Xoshiro& r, double& nr
   nim = __dmul_rn(rad, sn);
 }
 
+// demap_f64 (below) for a constellation of M points known at compile time: the M
+// metrics once per symbol in registers, and exp(metric - max) once per symbol for the
+// halves whose maximum is the symbol's largest metric.  Every value is computed by the
+// same operations from the same operands as in demap_f64, so the LLRs are identical.
+template <int M, typename Put>
+__device__ __forceinline__ void demap_f64_fixed(const double* pts, double log_m, bool exact, double yre, double yim,
+                                                double sigma2, int n_bits, Put&& put) {
+  constexpr int MB = M == 4 ? 2 : (M == 16 ? 4 : (M == 64 ? 6 : 8));
+  const double uniform = -log_m;
+  double met[M];
+  double top = -INFINITY;
+#pragma unroll
+  for (int i = 0; i < M; i++) {
+    const double dr = __dsub_rn(yre, pts[2 * i]), di = __dsub_rn(yim, pts[2 * i + 1]);
+    const double ns = __dadd_rn(__dmul_rn(dr, dr), __dmul_rn(di, di));
+    met[i] = __dadd_rn(__ddiv_rn(-ns, sigma2), uniform);
+    top = fmax(top, met[i]);
+  }
+  double ex[M];
+  if (exact && isfinite(top)) {
+#pragma unroll
+    for (int i = 0; i < M; i++) ex[i] = exp(__dsub_rn(met[i], top));
+  }
+#pragma unroll
+  for (int o = 0; o < MB; o++) {
+    if (o >= n_bits) break;
+    const int shift = MB - 1 - o;
+    double m0 = -INFINITY, m1 = -INFINITY;
+#pragma unroll
+    for (int i = 0; i < M; i++) {
+      if ((i >> shift) & 1) m1 = fmax(m1, met[i]);
+      else m0 = fmax(m0, met[i]);
+    }
+    if (exact && isfinite(m0) && isfinite(m1)) {
+      double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+      for (int i = 0; i < M; i++) {
+        if ((i >> shift) & 1) s1 = __dadd_rn(s1, m1 == top ? ex[i] : exp(__dsub_rn(met[i], m1)));
+        else s0 = __dadd_rn(s0, m0 == top ? ex[i] : exp(__dsub_rn(met[i], m0)));
+      }
+      put(o, __dsub_rn(__dsub_rn(__dadd_rn(m0, log(s0)), m1), log(s1)));
+    } else {
+      put(o, __dsub_rn(m0, m1));
+    }
+  }
+}
+
 // The LLRs of the mbits bits of one symbol y, most significant first
 // (crates/com-mapping/src/demapper.rs:82-146, :270-297): metric_i = -|y - x_i|^2 /
 // sigma^2 - ln M; max-log L = max_{b=0} - max_{b=1}; exact (LabelHalves) the sums of
 // exp(metric - max) in label order, L = m0 + ln s0 - m1 - ln s1, with CUDA's exp and
 // log where the reference calls libm.  put(o, L) receives bit o's LLR; bits at o >=
 // n_bits are skipped.
+// QPSK and 16-QAM take demap_f64_fixed.
 template <typename Put>
 __device__ __forceinline__ void demap_f64(const double* pts, int m, int mbits, double log_m, bool exact, double yre,
                                           double yim, double sigma2, int n_bits, Put&& put) {
+  if (m == 4) return demap_f64_fixed<4>(pts, log_m, exact, yre, yim, sigma2, n_bits, put);
+  if (m == 16) return demap_f64_fixed<16>(pts, log_m, exact, yre, yim, sigma2, n_bits, put);
   const double uniform = -log_m;
   for (int o = 0; o < mbits && o < n_bits; o++) {
     const int shift = mbits - 1 - o;
