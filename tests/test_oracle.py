@@ -200,3 +200,18 @@ def test_exact_demapper_is_the_log_sum_exp_of_the_label_halves(O, m):
         assert np.allclose(got, ml, rtol=1e-13, atol=1e-13)
     else:
         assert not np.allclose(got, ml)
+
+
+def test_counts_do_not_depend_on_the_thread_count(O):
+    # every frame draws from its own stream (runner.rs:435-447), so the records are the
+    # same whatever the number of worker threads
+    code = O.Code(520, 1040, 2, 52).set_decoder(O.RULE_NMS, 0.75, True, 20)
+    h = O.fnv1a64("bicm_ldpc")
+    one = code.run_frames(4, 7, h, 2, 100, 64, 1.0, 0, O.NOISE_CR, 1)
+    many = code.run_frames(4, 7, h, 2, 100, 64, 1.0, 0, O.NOISE_CR, 4)
+    assert np.array_equal(one, many)
+    peg = O.Code(alist=open(os.path.join(GOLDEN, "peg_n576_k288.alist")).read())
+    peg.set_decoder(O.RULE_NMS, 0.75, True, 20)
+    a, _, _ = peg.link_trials(2, 0, 16, 6, h, 0, 0, 24, 3.0, threads=1)
+    b, _, _ = peg.link_trials(2, 0, 16, 6, h, 0, 0, 24, 3.0, threads=4)
+    assert np.array_equal(a, b)
