@@ -27,7 +27,6 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <algorithm>
 #include <cstdio>
 
 #include "decode_common.cuh"
@@ -55,12 +54,9 @@ __host__ __device__ __forceinline__ size_t decode_smem_bytes(int n_full, int z, 
 // in the launch parameters, or each iteration's staged in shared memory
 enum LearnedWeights { kPlain = 0, kWeightsGlobal = 1, kWeightsParam = 2, kWeightsShared = 3 };
 
-// TM: the row state of the first a.tmem_layers layers lives in tensor memory (f32 plain
-// decoder, Z a multiple of 32 so that every warp's threads are all active)
-template <typename T, int LW, bool TM = false>
+template <typename T, int LW>
 __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float* la, const float* lb) {
   constexpr bool LEARNED = LW != kPlain;
-  static_assert(!TM || (sizeof(T) == 4 && !LEARNED), "tensor-memory state: f32 plain decoder only");
   extern __shared__ __align__(16) unsigned char smem[];
   const cbd::DevCode& c = a.code;
   const int z = c.z, nt = blockDim.x, tid = threadIdx.x;
@@ -81,19 +77,6 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
   const bool active = tid < z;
   for (int i = tid; i < c.n_entries; i += nt) s_ent[i] = c.entry[i];
   for (int i = tid; i <= c.rows_n; i += nt) s_lstart[i] = c.layer_start[i];
-  // tensor memory: layer L < t_layers keeps its row record at column t_col + 4 L of the
-  // thread's lane
-  uint32_t t_base = 0, t_row = 0;
-  int t_layers = 0;
-  if constexpr (TM) {
-    __shared__ uint32_t s_tmem;
-    const int warp = tid >> 5;
-    if (warp == 0) tmem_alloc(&s_tmem, (uint32_t)a.tmem_cols);
-    tmem_cta_sync();
-    t_base = s_tmem;
-    t_row = t_base + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * a.tmem_group_cols);
-    t_layers = a.tmem_layers;
-  }
 
   for (;;) {
     if (tid == 0) {
@@ -178,14 +161,7 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
           const int L = c.layer_order[q];
           T a1 = (T)0, a2 = (T)0;
           uint32_t mt = 0;
-          if (iter > 1 && active) {
-            if constexpr (TM) {
-              if (L < t_layers) tmem_load_row(t_row + 4 * L, a1, a2, mt);
-              else st.load(L * z + tid, a1, a2, mt);
-            } else {
-              st.load(L * z + tid, a1, a2, mt);
-            }
-          }
+          if (iter > 1 && active) st.load(L * z + tid, a1, a2, mt);
           if (active) {
             const int s0 = c.layer_start[L];
             const int d = c.layer_start[L + 1] - s0;
@@ -200,16 +176,10 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
                                 n1, n2, nm);
             else
               row_dispatch<T>(d, post, c.entry + s0, tid, z, a1, a2, mt, rule, alpha, n1, n2, nm);
-            if constexpr (TM) {
-              if (L < t_layers) tmem_store_row(t_row + 4 * L, n1, n2, nm);
-              else st.store(L * z + tid, n1, n2, nm);
-            } else {
-              st.store(L * z + tid, n1, n2, nm);
-            }
+            st.store(L * z + tid, n1, n2, nm);
           }
           if (c.level_end[q]) __syncthreads();
         }
-        if constexpr (TM) tmem_wait_st();
         if (!some_check_fails(post, hd, s_ent, s_lstart, c.rows_n, ncol, z, tid, nt)) {
           it = iter;
           break;
@@ -249,20 +219,11 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
     }
     __syncthreads();
   }
-  if constexpr (TM) {
-    tmem_cta_sync();
-    if ((tid >> 5) == 0) tmem_dealloc(t_base, (uint32_t)a.tmem_cols);
-  }
 }
 
 template <typename T, int LW>
 __global__ void __launch_bounds__(384, sizeof(T) == 4 ? 2 : 1) layered_kernel(const __grid_constant__ DecodeArgs<T> a) {
   decode_body<T, LW>(a, a.l_alpha, a.l_beta);
-}
-
-// the f32 plain decoder with part of its row state in tensor memory
-__global__ void __launch_bounds__(384, 2) layered_tmem_kernel(const __grid_constant__ DecodeArgs<float> a) {
-  decode_body<float, kPlain, true>(a, nullptr, nullptr);
 }
 
 __global__ void __launch_bounds__(384, 2) layered_learned_param_kernel(const __grid_constant__ LearnedParamArgs a) {
@@ -306,35 +267,9 @@ cudaError_t launch_decode(const DecodeArgs<T>& a, int grid, cudaStream_t stream)
   const int precision = sizeof(T) == 8 ? 0 : 1;
   void* k = kernel_for<T>(a);
   size_t smem = smem_bytes(a.code, precision) + (a.l_smem ? (size_t)4 * 4 * a.code.n_entries : 0);
-  DecodeArgs<T> b = a;
-  b.tmem_cols = b.tmem_layers = b.tmem_group_cols = 0;
-  if constexpr (sizeof(T) == 4) {
-    // the plain f32 decoder with every warp full keeps part of its row state in tensor
-    // memory: the 512 columns of an SM shared by the CTAs resident on it, each warp group
-    // (four warps, the 128 lanes) a quarter-aligned range of its CTA's columns
-    if (!a.l_alpha && a.code.z % 32 == 0) {
-      void* kt = (void*)layered_tmem_kernel;
-      cudaError_t e = cudaFuncSetAttribute(kt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      int per_sm = 0;
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kt, block_threads(a.code.z), smem);
-      if (e != cudaSuccess) return e;
-      int cols = 512;
-      while (per_sm > 0 && cols * per_sm > 512) cols >>= 1;
-      const int groups = (block_threads(a.code.z) / 32 + 3) / 4;
-      const int group_cols = (cols / groups) & ~3;
-      const int layers = std::min(a.code.rows_n, group_cols / 4);
-      if (per_sm > 0 && cols >= 32 && layers > 0) {
-        b.tmem_cols = cols;
-        b.tmem_group_cols = group_cols;
-        b.tmem_layers = layers;
-        k = kt;
-      }
-    }
-  }
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  void* args[] = {(void*)&b};
+  void* args[] = {(void*)&a};
   return cudaLaunchKernel(k, dim3(grid), dim3(block_threads(a.code.z)), args, smem, stream);
 }
 

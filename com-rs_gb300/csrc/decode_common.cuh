@@ -380,44 +380,6 @@ __device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent
 // {n1, n2} record plus a plane of meta words
 template <typename T>
 struct StateSlot;
-// ---- tensor memory as a per-thread store of row state (tcgen05, sm_100 family).  A warp
-// reaches the 32 TMEM lanes of its quarter of the CTA (warp index mod 4), so thread i of
-// warp w owns lane 32 (w mod 4) + i and the column range of its warp group (w / 4).
-// One warp allocates and frees the CTA's columns; tcgen05.ld results are valid after
-// tcgen05.wait::ld, which the registers are passed through so that no use moves above it.
-__device__ __forceinline__ void tmem_alloc(uint32_t* smem_dst, uint32_t ncols) {
-  const uint32_t dst = (uint32_t)__cvta_generic_to_shared(smem_dst);
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(ncols) : "memory");
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-// a CTA barrier that orders the tensor-memory operations before it with those after it
-__device__ __forceinline__ void tmem_cta_sync() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-// a row record {n1, n2, meta, unused} in four consecutive columns of the thread's lane
-__device__ __forceinline__ void tmem_load_row(uint32_t taddr, float& a1, float& a2, uint32_t& mt) {
-  uint32_t x, y, w, u;
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
-               : "=r"(x), "=r"(y), "=r"(w), "=r"(u)
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(x), "+r"(y), "+r"(w), "+r"(u)::"memory");
-  a1 = __uint_as_float(x);
-  a2 = __uint_as_float(y);
-  mt = w;
-}
-__device__ __forceinline__ void tmem_store_row(uint32_t taddr, float n1, float n2, uint32_t nm) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr), "r"(__float_as_uint(n1)),
-               "r"(__float_as_uint(n2)), "r"(nm), "r"(0u)
-               : "memory");
-}
-// the thread's earlier tensor-memory stores are complete (before it reads them back)
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-
 // The state records of all resident CTAs (64 MB at BG1 Z = 384) fit in L2, but the LLR
 // stream of a launch (830 MB for 8192 codewords) would evict them: the records are read
 // and written with an L2 evict-last policy, the LLRs with streaming loads.

@@ -30,12 +30,6 @@ struct DecodeArgs {
   const float* l_beta = nullptr;
   int32_t l_shared = 0;
   int32_t l_smem = 0;  // 1: each iteration's (shared) weights staged in shared memory
-  // the f32 plain decoder keeps the row state of its first tmem_layers layers in tensor
-  // memory: tmem_cols columns per CTA, tmem_group_cols for each group of four warps
-  // (set by launch_decode; 0: all the state in global memory)
-  int32_t tmem_cols = 0;
-  int32_t tmem_layers = 0;
-  int32_t tmem_group_cols = 0;
 };
 
 // The learned decoder with its weights in the launch parameters (weights shared across
