@@ -177,7 +177,14 @@ class Ldpc:
     # ------------------------------------------------------------------ constructors
     @classmethod
     def peg(cls, n, k, *, var_degree=DEFAULT_VAR_DEGREE, seed=DEFAULT_PEG_SEED, **kw):
-        """``LdpcCode.peg(n, k, var_degree=3, seed=1)``: progressive edge growth."""
+        """``LdpcCode.peg(n, k, var_degree=3, seed=1)``: progressive edge growth.
+
+        >>> import importlib
+        >>> cb = importlib.import_module("com-rs_gb300")
+        >>> code = cb.Ldpc.peg(96, 48)
+        >>> code.n, code.k, code.girth() >= 6
+        (96, 48, True)
+        """
         return cls(n, peg_rows(n, k, var_degree, seed), **kw)
 
     @classmethod
@@ -322,7 +329,13 @@ class Ldpc:
 
     def encode(self, bits):
         """Encode whole blocks: a multiple of `k` bits (1-D, the coded blocks one after
-        the other) or rows of `k` bits (2-D, one coded block per row), on the GPU."""
+        the other) or rows of `k` bits (2-D, one coded block per row), on the GPU.
+
+        >>> import importlib, numpy as np
+        >>> cb = importlib.import_module("com-rs_gb300")
+        >>> cb.Ldpc.peg(96, 48).encode(np.random.default_rng(1).integers(0, 2, 96)).size  # doctest: +SKIP
+        192
+        """
         k = self.k
         u = np.ascontiguousarray(bits, np.uint8)
         u2 = self._blocks(u, k, "bits")
@@ -348,7 +361,15 @@ class Ldpc:
     def decode(self, llr):
         """Decode whole blocks of LLRs (positive for a 0): a multiple of `n` (1-D, the
         `k` decided information bits of every block one after the other) or rows of `n`
-        (2-D, one row of `k` bits per block)."""
+        (2-D, one row of `k` bits per block).
+
+        >>> import importlib, numpy as np
+        >>> cb = importlib.import_module("com-rs_gb300")
+        >>> code = cb.Ldpc.peg(96, 48)
+        >>> b = np.random.default_rng(1).integers(0, 2, 48).astype(np.uint8)
+        >>> bool(np.array_equal(code.decode(2.0 - 4.0 * code.encode(b)), b))  # doctest: +SKIP
+        True
+        """
         x = np.ascontiguousarray(llr, self.dtype)
         x2 = self._blocks(x, self._n, "llr")
         post, _ = self.decode_llr(x2)

@@ -212,3 +212,15 @@ def test_block_shapes_are_checked(cb):
         code.encode(np.zeros(6, np.uint8))
     with pytest.raises(ValueError, match="expected 7"):
         code.decode(np.zeros((2, 6)))
+
+
+def test_docstring_examples(cb):
+    # the examples of Ldpc (the reference's LdpcCode examples, bindings/com-py/src/fec/
+    # ldpc_code.rs:51-54, :130-156); those that need a GPU are skipped here and run in
+    # tests/test_gpu_sparse.py
+    import doctest
+
+    finder, runner = doctest.DocTestFinder(), doctest.DocTestRunner(optionflags=doctest.ELLIPSIS)
+    for t in finder.find(cb.Ldpc, "Ldpc"):
+        runner.run(t)
+    assert runner.failures == 0 and runner.tries >= 6
