@@ -18,6 +18,12 @@ against the measured HBM copy bandwidth.
 --impl reference: the CPU oracle's restatement of the reference trial (f64, the
 reference's libm noise) on all host cores, a bounded sample of frames per step.
 
+--workload mix: the uneven mixed batch: 16,384 codewords, each of a base graph, lifting size
+Z, rate, modulation and Eb/N0 drawn uniformly (BG {1, 2}, Z {16, 32, 64, 128, 208, 384},
+R {1/3, 1/2, 2/3, 5/6}, QPSK to 256-QAM, 0 to 6 dB), f32, at most 25 iterations, generated
+and decoded by one replayed CUDA graph with per-codeword early exit and work stealing;
+rows per thread autotuned.  One step = one replay on the next frames of every item.
+
 --workload spec: the link of com-rs's specs/bicm_ldpc.yaml instead (fec_encode of a PEG
 (1024, 512) code, 8 blocks per trial, random interleaver, Gray 16-QAM, awgn_ebn0, exact
 LLRs, layered sum-product with 50 iterations, f64), Eb/N0 2.5:0.5:5 dB, `--trials` trials
@@ -492,6 +498,147 @@ def run_spec_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+MIX_N, MIX_ITEMS_SEED, MIX_SEED, MIX_NAME = 16384, 2024, 7, "bicm_ldpc_mix"
+MIX_METRIC = "decoded info Gbit/s of the uneven mixed batch (one graph replay per step); vs CPU Runner"
+MIX_WORKLOAD = ("16,384 codewords per replay, each: BG {1,2}, Z {16,32,64,128,208,384}, R {1/3,1/2,2/3,5/6}, "
+                "Gray QPSK..256-QAM, Eb/N0 U[0,6] dB (item seed 2024); f32, layered NMS alpha=0.75, <=25 "
+                "iterations with per-codeword early exit; one persistent decoder with work stealing, CUDA graph")
+
+
+def mix_cpu_sample(budget_s, threads=0):
+    """The oracle's trial (f64, libm noise) of the mixed batch's items, one frame each,
+    over all host threads (the oracle releases the interpreter lock), for about
+    budget_s seconds: (Gbit/s, cores, items, seconds)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    cb = importlib.import_module("com-rs_gb300")
+    items = cb.draw_mixed_batch(n=MIX_N, seed=MIX_ITEMS_SEED)
+    cores = threads or os.cpu_count()
+    h = O.fnv1a64(MIX_NAME)
+    codes = {}
+
+    def code_of(it):
+        key = (int(it["base_graph"]), int(it["lifting_size"]), int(it["k_info"]), int(it["e"]))
+        if key not in codes:
+            codes[key] = O.Code(key[2], key[3], bg=key[0], z=key[1]).set_decoder(O.RULE_NMS, 0.75, True, 25)
+        return codes[key]
+
+    def one(i):
+        it = items[i]
+        code_of(it).trial(int(it["modulation_order"]), MIX_SEED, h, int(it["condition"]), int(it["frame"]),
+                          float(it["ebn0_db"]), 0, O.NOISE_LIBM)
+        return int(it["k_info"])
+
+    for it in items:  # every code's host tables first, outside the timed sample
+        code_of(it)
+    done, bits, t0 = 0, 0, time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        while time.perf_counter() - t0 < budget_s and done < MIX_N:
+            n = min(4 * cores, MIX_N - done)
+            bits += sum(ex.map(one, range(done, done + n)))
+            done += n
+    t = time.perf_counter() - t0
+    return bits / t / 1e9, cores, done, t
+
+
+def run_mix_reference(args, rank):
+    if rank != 0:
+        return
+    gbps, cores, done, t = mix_cpu_sample(max(2.0, 3.0 * args.steps))
+    line = {"impl": "reference", "metric": MIX_METRIC, "value": gbps, "unit": "Gbit/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": MIX_WORKLOAD, "items_sampled": done},
+            "cpu_baseline": {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port",
+                             "sample": f"the first {done} items of the batch, one frame each ({t:.1f} s), f64 decoder "
+                                       f"and libm noise as the reference"},
+            "e2e": {"value": gbps, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_mix_ours(args, rank, world, local_rank):
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    cb = importlib.import_module("com-rs_gb300")
+    items = cb.draw_mixed_batch(n=MIX_N, seed=MIX_ITEMS_SEED)
+    mix = cb.MixBatch(items, seed=MIX_SEED, name=MIX_NAME, max_iterations=25, device=local_rank)
+    tuned = cb.autotune(mix, reps=2, cache=False)
+    bits = int(items["k_info"].sum())
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for s in range(args.warmup):
+        mix.run(epoch=10_000 + s)
+    barrier()
+    fer = []
+    with ClockSampler(local_rank) as clocks:
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            rec = mix.run(epoch=s * world + rank)
+            fer.append(float(rec["frame_error"].mean()))
+        barrier()
+        wall = max_over_ranks(time.perf_counter() - t0)
+    value = args.steps * world * bits / wall / 1e9
+    # the decode phase alone, event-timed inside the library, against HBM
+    dec_ms = mix.time_decode(-1, reps=3)
+    algo = int((items["e"].astype(np.int64) * 4 + (items["k_info"].astype(np.int64) + 7) // 8 + 4).sum())
+    peaks = read_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = algo / (dec_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "mix_decode_kernel (decode phase of a replay)",
+                "algorithmic_bytes_per_launch": algo, "launch_ms": dec_ms,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+                "note": "issue-bound like the single-code decoder; the HBM fraction is the algorithmic-bytes one"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        gbps, cores, done, t = mix_cpu_sample(10.0)
+        cpu = {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port",
+               "sample": f"the first {done} items of the batch, one frame each ({t:.1f} s), f64 decoder and libm "
+                         f"noise as the reference"}
+    if rank == 0:
+        e2e = {"value": value, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": MIX_N * 8,
+               "api": "cb_mix_run (graph replay, records to the host)",
+               "inputs": "the items' streams (seed, name, condition, frame + epoch x items)"}
+        line = {"metric": MIX_METRIC, "value": value, "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (Monte Carlo frames from seeded streams)",
+                "config": {"workload": MIX_WORKLOAD, "codewords_per_step": MIX_N, "info_bits_per_step": bits,
+                           "rows_per_thread": {str(z): v[0] for z, v in tuned.items()},
+                           "timing": "host clock around the synchronous replay call (device work and the 128 KB "
+                                     "of records); value and e2e are the same measurement",
+                           "l2": "each replay writes and reads its LLRs once; no flush between replays",
+                           "parallelism": f"dp{world} (disjoint epochs per GPU)",
+                           "mean_fer": float(np.mean(fer))},
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
+                "gpu_launches": 2 * args.steps}
+        print(json.dumps(line), flush=True)
+    mix.close()
+    if dist:
+        dist.destroy_process_group()
+
+
 def run_spec_profile_case(args):
     """The small case of the spec link for ncu: `trials` trials generated once at 2.5 dB,
     their codewords then decoded three times by the f64 and three times by the f32
@@ -555,8 +702,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--frames", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["c2", "spec"], default="c2",
-                    help="c2: the NR trial (the headline); spec: the link of specs/bicm_ldpc.yaml")
+    ap.add_argument("--workload", choices=["c2", "mix", "spec"], default="c2",
+                    help="c2: the NR trial (the headline); mix: the uneven mixed batch; spec: the link of "
+                         "specs/bicm_ldpc.yaml")
     ap.add_argument("--trials", type=int, default=2048, help="trials per step of --workload spec")
     ap.add_argument("--profile-case", action="store_true",
                     help="generate --frames C2 codewords (--workload spec: --trials trials) and decode them "
@@ -576,6 +724,11 @@ def main():
             run_spec_reference(args, rank)
         else:
             run_spec_ours(args, rank, world, local_rank)
+    elif args.workload == "mix":
+        if args.impl == "reference":
+            run_mix_reference(args, rank)
+        else:
+            run_mix_ours(args, rank, world, local_rank)
     elif args.impl == "reference":
         run_reference(args, rank)
     else:
