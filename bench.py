@@ -24,6 +24,12 @@ R {1/3, 1/2, 2/3, 5/6}, QPSK to 256-QAM, 0 to 6 dB), f32, at most 25 iterations,
 and decoded by one replayed CUDA graph with per-codeword early exit and work stealing;
 rows per thread autotuned.  One step = one replay on the next frames of every item.
 
+--workload learned (--protocol c5 or c4): decoded info Gbit/s at equal FER, neural vs plain
+min-sum.  The learned min-sum with the weights the committed protocol trained
+(com-rs_gb300/weights/, from `python com-rs_gb300/learned.py c5|c4`) runs at its FER 1e-3
+Eb/N0; the plain min-sum at 20 iterations and at the learned decoder's iteration count
+run at theirs (measured on the protocol's curves).  `value` is the learned decoder's.
+
 --workload spec: the link of com-rs's specs/bicm_ldpc.yaml instead (fec_encode of a PEG
 (1024, 512) code, 8 blocks per trial, random interleaver, Gray 16-QAM, awgn_ebn0, exact
 LLRs, layered sum-product with 50 iterations, f64), Eb/N0 2.5:0.5:5 dB, `--trials` trials
@@ -639,6 +645,153 @@ def run_mix_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+# the Eb/N0 (dB) of FER 1e-3 on the protocol's curves, for the learned decoder, the plain
+# decoder at 20 iterations and the plain decoder at the learned one's iteration count
+LEARNED_POINTS = {"c5": {"learned": 6.97, "plain_20": 6.51, "plain_T": 7.33},
+                  "c4": {"learned": 2.17, "plain_20": 2.09, "plain_T": 2.35}}
+LEARNED_FRAMES = {"c5": 8192, "c4": 65536}
+LEARNED_METRIC = "decoded info Gbit/s at equal FER (1e-3), neural vs plain min-sum; vs CPU Runner"
+
+
+def learned_setup(proto):
+    cb = importlib.import_module("com-rs_gb300")
+    Lm = importlib.import_module("com-rs_gb300.learned")
+    p = Lm.PROTOCOLS[proto]
+    return cb, Lm, p
+
+
+def learned_workload(p, proto):
+    return (f"{proto}: BG{p['bg']} Z={p['z']} K'={p['k']} E={p['e']}, Gray {p['m']}-QAM; learned min-sum "
+            f"({p['T']} iterations, weights shared per base edge, trained by the protocol) at its FER 1e-3 Eb/N0 "
+            f"against plain NMS alpha=0.75 at 20 and at {p['T']} iterations at theirs; f32, syndrome stop")
+
+
+def learned_cpu_sample(proto, budget_s, threads=0):
+    """The oracle's plain 20-iteration decoder (f64, libm noise: the reference, which has
+    no learned decoder) at its FER 1e-3 point, over all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    _, _, p = learned_setup(proto)
+    cores = threads or os.cpu_count()
+    code = O.Code(p["k"], p["e"], bg=p["bg"], z=p["z"]).set_decoder(O.RULE_NMS, 0.75, True, 20)
+    h = O.fnv1a64("learned_bench")
+    eb = LEARNED_POINTS[proto]["plain_20"]
+    t0 = time.perf_counter()
+    code.run_frames(p["m"], 1, h, 0, 0, cores, eb, 0, O.NOISE_LIBM, cores)
+    per = (time.perf_counter() - t0) / cores
+    n = max(cores, int(budget_s / per / cores) * cores)
+    t0 = time.perf_counter()
+    r = code.run_frames(p["m"], 1, h, 0, cores, n, eb, 0, O.NOISE_LIBM, cores)
+    t = time.perf_counter() - t0
+    return n * p["k"] / t / 1e9, cores, n, t, float(r["frame_error"].mean())
+
+
+def run_learned_reference(args, rank):
+    if rank != 0:
+        return
+    _, _, p = learned_setup(args.protocol)
+    gbps, cores, n, t, fer = learned_cpu_sample(args.protocol, max(2.0, 2.0 * args.steps))
+    line = {"impl": "reference", "metric": LEARNED_METRIC, "value": gbps, "unit": "Gbit/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": learned_workload(p, args.protocol), "frames": n, "fer": fer},
+            "cpu_baseline": {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port",
+                             "sample": f"{n} frames ({t:.1f} s) of the plain 20-iteration decoder at its FER 1e-3 "
+                                       f"point, f64 and libm noise as the reference (which has no learned decoder)"},
+            "e2e": {"value": gbps, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_learned_ours(args, rank, world, local_rank):
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    cb, Lm, p = learned_setup(args.protocol)
+    B = LEARNED_FRAMES[args.protocol]
+    pts = LEARNED_POINTS[args.protocol]
+
+    def nr(it):
+        return cb.NrLdpc(p["k"], p["e"], base_graph=p["bg"], lifting_size=p["z"], precision="f32",
+                         max_iterations=it, device=local_rank)
+
+    code = nr(p["T"])
+    net = cb.LearnedNms(code, p["T"], shared=p["shared"])
+    Lm.load(net, os.path.join(ROOT, "com-rs_gb300", "weights", f"learned_{args.protocol}.npz"))
+    decoders = {"learned": (net.run_frames, pts["learned"]), "plain_20": (nr(20).run_frames, pts["plain_20"]),
+                f"plain_{p['T']}": (nr(p["T"]).run_frames, pts["plain_T"])}
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    out, clocks_summary = {}, None
+    for key, (run, eb) in decoders.items():
+        for s in range(args.warmup):
+            run(3, "learned_bench", 1, 10_000_000 + s * B, B, eb, p["m"])
+        barrier()
+        recs = []
+        with ClockSampler(local_rank) as clocks:
+            t0 = time.perf_counter()
+            for s in range(args.steps):
+                recs.append(run(3, "learned_bench", 0, (s * world + rank) * B, B, eb, p["m"]))
+            barrier()
+            wall = max_over_ranks(time.perf_counter() - t0)
+        r = np.concatenate(recs)
+        out[key] = {"value": args.steps * world * B * p["k"] / wall / 1e9, "unit": "Gbit/s", "ebn0_db": eb,
+                    "fer": float(r["frame_error"].mean()), "frame_errors": int(r["frame_error"].sum()),
+                    "frames": int(len(r)) * world, "mean_iterations": float(r["iterations"].mean()),
+                    "ms_per_step": wall / args.steps * 1e3}
+        if key == "learned":
+            clocks_summary = clocks.summary()
+    lv = out["learned"]
+    algo = B * (p["e"] * 4 + (p["k"] + 7) // 8 + 4)
+    peaks = read_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = algo / (lv["ms_per_step"] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "layered learned decoder, timed with the frame generator (one step)",
+                "algorithmic_bytes_per_launch": algo, "launch_ms": lv["ms_per_step"],
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+                "note": "issue-bound like the plain decoder; the step includes the generator"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        gbps, cores, n, t, fer = learned_cpu_sample(args.protocol, 5.0)
+        cpu = {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port",
+               "sample": f"{n} frames ({t:.1f} s) of the plain 20-iteration decoder at its FER 1e-3 point (FER "
+                         f"{fer:.1e}), f64 and libm noise as the reference (which has no learned decoder)"}
+    if rank == 0:
+        line = {"metric": LEARNED_METRIC, "value": lv["value"], "unit": "Gbit/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": lv["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (Monte Carlo frames from seeded streams)",
+                "config": {"workload": learned_workload(p, args.protocol), "frames_per_step": B,
+                           "decoders": out, "timing": "host clock around cb_nms_run_frames / cb_run_frames "
+                                                       "(generation, decoding, records to the host)",
+                           "parallelism": f"dp{world} (disjoint frame ranges per GPU)"},
+                "e2e": {"value": lv["value"], "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": B * 8,
+                        "api": "cb_nms_run_frames (records to the host)"},
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks_summary,
+                "gpu_launches": 2 * args.steps}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def run_spec_profile_case(args):
     """The small case of the spec link for ncu: `trials` trials generated once at 2.5 dB,
     their codewords then decoded three times by the f64 and three times by the f32
@@ -702,9 +855,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--frames", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["c2", "mix", "spec"], default="c2",
-                    help="c2: the NR trial (the headline); mix: the uneven mixed batch; spec: the link of "
-                         "specs/bicm_ldpc.yaml")
+    ap.add_argument("--workload", choices=["c2", "mix", "learned", "spec"], default="c2",
+                    help="c2: the NR trial (the headline); mix: the uneven mixed batch; learned: neural vs plain "
+                         "min-sum at equal FER; spec: the link of specs/bicm_ldpc.yaml")
+    ap.add_argument("--protocol", choices=["c5", "c4"], default="c5", help="the code of --workload learned")
     ap.add_argument("--trials", type=int, default=2048, help="trials per step of --workload spec")
     ap.add_argument("--profile-case", action="store_true",
                     help="generate --frames C2 codewords (--workload spec: --trials trials) and decode them "
@@ -729,6 +883,11 @@ def main():
             run_mix_reference(args, rank)
         else:
             run_mix_ours(args, rank, world, local_rank)
+    elif args.workload == "learned":
+        if args.impl == "reference":
+            run_learned_reference(args, rank)
+        else:
+            run_learned_ours(args, rank, world, local_rank)
     elif args.impl == "reference":
         run_reference(args, rank)
     else:
