@@ -187,7 +187,9 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
       }
     }
 
-    // ---- outputs: hard decisions (signal.rs:47-49), counts (errors.rs:39-42)
+    // ---- outputs: hard decisions (signal.rs:47-49), counts (errors.rs:39-42).  The words
+    // of decisions are staged in hd (free after the syndrome test) and written 16 bytes at
+    // a time when the row of words allows it.
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     unsigned int be = 0;
     for (int b0 = warp * 32; b0 < c.k_info; b0 += nw * 32) {
@@ -195,9 +197,17 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
       bool bit = v < c.k_info && post[v] < (T)0;
       uint32_t word = __ballot_sync(0xffffffffu, bit);
       if (lane == 0) {
-        size_t w = (size_t)cw * wpf + (b0 >> 5);
-        if (a.bits_out) a.bits_out[w] = word;
-        if (a.ref_bits) be += __popc(word ^ a.ref_bits[w]);
+        hd[b0 >> 5] = word;
+        if (a.ref_bits) be += __popc(word ^ a.ref_bits[(size_t)cw * wpf + (b0 >> 5)]);
+      }
+    }
+    __syncthreads();
+    if (a.bits_out) {
+      uint32_t* dst = a.bits_out + (size_t)cw * wpf;
+      if ((wpf & 3) == 0 && (reinterpret_cast<uintptr_t>(a.bits_out) & 15) == 0) {
+        for (int q = tid; q < (wpf >> 2); q += nt) reinterpret_cast<uint4*>(dst)[q] = reinterpret_cast<const uint4*>(hd)[q];
+      } else {
+        for (int w = tid; w < wpf; w += nt) dst[w] = hd[w];
       }
     }
     if (a.app_out)
