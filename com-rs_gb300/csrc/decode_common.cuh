@@ -130,17 +130,41 @@ __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t*
   // check_message, min-sum branch (ldpc.rs:468-491): sign product with `l < 0`, strict
   // `<` for the minimum and its index, min(m2, a) for the second (equal for non-NaN,
   // and a NaN is skipped by both)
-  uint32_t par = (uint32_t)(x[0] < (T)0);
-  T m1 = fmin(fabs(x[0]), infinity<T>()), m2 = infinity<T>();
+  uint32_t par;
+  T m1, m2;
   int i1 = 0;
+  if constexpr (sizeof(T) == 8) {
+    // f64 on the integer pipes: the posteriors and messages are never -0.0 or NaN, so
+    // `l < 0` is the sign bit, and the order of non-negative doubles is that of their
+    // bit patterns; only the subtractions and additions stay on the FP64 pipe
+    const long long kAbs = 0x7fffffffffffffffll;
+    par = (uint32_t)((unsigned long long)__double_as_longlong(x[0]) >> 63);
+    long long b1 = __double_as_longlong(x[0]) & kAbs, b2 = 0x7ff0000000000000ll;
 #pragma unroll
-  for (int e = 1; e < D; e++) {
-    par ^= (uint32_t)(x[e] < (T)0);
-    T av = fabs(x[e]);
-    bool lt = av < m1;
-    m2 = lt ? m1 : fmin(m2, av);
-    m1 = lt ? av : m1;
-    i1 = lt ? e : i1;
+    for (int e = 1; e < D; e++) {
+      const long long bx = __double_as_longlong(x[e]);
+      par ^= (uint32_t)((unsigned long long)bx >> 63);
+      const long long av = bx & kAbs;
+      const bool lt = av < b1;
+      b2 = lt ? b1 : (av < b2 ? av : b2);
+      b1 = lt ? av : b1;
+      i1 = lt ? e : i1;
+    }
+    m1 = __longlong_as_double(b1);
+    m2 = __longlong_as_double(b2);
+  } else {
+    par = (uint32_t)(x[0] < (T)0);
+    m1 = fmin(fabs(x[0]), infinity<T>());
+    m2 = infinity<T>();
+#pragma unroll
+    for (int e = 1; e < D; e++) {
+      par ^= (uint32_t)(x[e] < (T)0);
+      T av = fabs(x[e]);
+      bool lt = av < m1;
+      m2 = lt ? m1 : fmin(m2, av);
+      m1 = lt ? av : m1;
+      i1 = lt ? e : i1;
+    }
   }
   if (rule == cbd::RULE_NMS) {
     n1 = mul_rn(alpha, m1);
@@ -152,9 +176,18 @@ __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t*
   nm = (uint32_t)i1;
 #pragma unroll
   for (int e = 0; e < D; e++) {
-    uint32_t ng = par ^ (uint32_t)(x[e] < (T)0);
-    T mag = (e == i1) ? n2 : n1;
-    T o = ng ? -mag : mag;
+    uint32_t ng;
+    T o;
+    if constexpr (sizeof(T) == 8) {
+      const long long bx = __double_as_longlong(x[e]);
+      ng = par ^ (uint32_t)((unsigned long long)bx >> 63);
+      const T mag = (e == i1) ? n2 : n1;
+      o = __longlong_as_double(__double_as_longlong(mag) ^ ((long long)ng << 63));
+    } else {
+      ng = par ^ (uint32_t)(x[e] < (T)0);
+      T mag = (e == i1) ? n2 : n1;
+      o = ng ? -mag : mag;
+    }
     post[off[e]] = add_rn(x[e], o);
     nm |= ng << (8 + e);
   }
