@@ -61,11 +61,11 @@ SEED, NAME = 7, "bicm_ldpc_c2"
 ALGO_BYTES = E * 4 + (K_INFO + 7) // 8 + 4
 # DRAM bytes (read + write) of the decoder per codeword at 20 iterations, and the
 # warp-instructions it issues per codeword and iteration, from one ncu capture of a
-# 2048-codeword launch (profiles/decode_c2_f32.md: 207,820,544 + 59,038,720 B,
-# smsp__inst_executed.sum = 5,009,431,744); the persistent grid keeps the same 304 state
+# 2048-codeword launch (profiles/decode_c2_f32.md: 208,447,232 + 71,422,976 B,
+# smsp__inst_executed.sum = 4,894,572,480); the persistent grid keeps the same 304 state
 # slots at any batch, so both scale by codewords
-DRAM_BYTES_PER_CODEWORD = (207_820_544 + 59_038_720) / 2048
-WARP_INST_PER_CODEWORD_ITERATION = 5_009_431_744 / (2048 * 20)
+DRAM_BYTES_PER_CODEWORD = (208_447_232 + 71_422_976) / 2048
+WARP_INST_PER_CODEWORD_ITERATION = 4_894_572_480 / (2048 * 20)
 WORKLOAD = ("5G NR LDPC BG1 Z=384 K'=8448 E=25344 (rate 1/3), Gray 16-QAM, AWGN Eb/N0 0:0.25:2 dB, "
             "max-log LLRs, layered NMS alpha=0.75, <=20 iterations + syndrome stop, f32, 8192 codewords/launch")
 
