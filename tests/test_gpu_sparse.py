@@ -306,3 +306,31 @@ def test_set_decoder_equals_a_fresh_code(cb, O):
         post_f, its_f = fresh.decode_llr(llr)
         assert np.array_equal(post.view(np.uint64), post_f.view(np.uint64)), rule
         assert np.array_equal(its, its_f), rule
+
+
+@pytest.mark.parametrize("n, m, dmax, seed", [(300, 150, 6, 1), (1200, 900, 5, 2), (2000, 600, 14, 3),
+                                              (4000, 2000, 8, 4)])
+def test_random_codes_equal_the_oracle(cb, O, n, m, dmax, seed):
+    # random rows (degree 2..dmax): levels of many rows (several codewords per CTA when
+    # they fit), rows longer than the register sum-product's 8 edges, messages in shared
+    # or global memory; min-sum bit for bit, sum-product by outcome
+    rng = np.random.default_rng(seed)
+    rows = [sorted(rng.choice(n, size=int(rng.integers(2, dmax + 1)), replace=False).tolist()) for _ in range(m)]
+    start = [0]
+    for r in rows:
+        start.append(start[-1] + len(r))
+    llr = rng.normal(2.0, 2.5, (96, n))
+    for precision, dt in (("f64", np.uint64), ("f32", np.uint32)):
+        gpu = cb.Ldpc(n, rows, rule="normalized_min_sum", alpha=0.75, max_iterations=15, precision=precision,
+                      encoder=None)
+        ref = O.Code(rows=rows, n=n)
+        ref.set_decoder(O.RULE_NMS, 0.75, True, 15)
+        post_g, it_g = gpu.decode_llr(llr)
+        post_o, it_o = ref.decode_llr_many(llr, precision)
+        assert np.array_equal(it_g, it_o), precision
+        assert np.array_equal(post_g.view(dt), post_o.view(dt)), precision
+    gpu = cb.Ldpc(n, rows, rule="sum_product", max_iterations=15, encoder=None)
+    ref.set_decoder(O.RULE_SUM_PRODUCT, 0.0, True, 15)
+    post_g, it_g = gpu.decode_llr(llr)
+    post_o, it_o = ref.decode_llr_many(llr, "f64")
+    assert ((post_g < 0) == (post_o < 0)).all(axis=1).mean() >= 0.95 and (it_g == it_o).mean() >= 0.9
