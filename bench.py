@@ -119,6 +119,33 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def start_ranks(world, local_rank):
+    """This process's GPU and, under torchrun, its NCCL process group: (dist or None,
+    barrier(), max_over_ranks(x)).  barrier() also synchronises the device."""
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return dist, barrier, max_over_ranks
+
+
 def cpu_sample(steps, warmup, threads=0, budget_s=2.0):
     """The oracle's trial (f64, libm noise, as the reference) over all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -164,12 +191,7 @@ def run_reference(args, rank):
 def run_ours(args, rank, world, local_rank):
     import torch
 
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    dist, barrier, max_over_ranks = start_ranks(world, local_rank)
     cb = importlib.import_module("com-rs_gb300")
     L = cb.lib()
     B = args.frames
@@ -186,18 +208,6 @@ def run_ours(args, rank, world, local_rank):
         st = L.cb_run_frames_device(h, M, SEED, nh, cond, first, B, GRID[cond], C.c_void_p(results.data_ptr()), sp)
         if st:
             raise cb.ComrsError(st, L.cb_last_error(h).decode())
-
-    def barrier():
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     for s in range(args.warmup):
         step(10_000 + s)
@@ -363,12 +373,7 @@ def run_spec_reference(args, rank):
 def run_spec_ours(args, rank, world, local_rank):
     import torch
 
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    dist, barrier, max_over_ranks = start_ranks(world, local_rank)
     cb = importlib.import_module("com-rs_gb300")
     L = cb.lib()
     T = args.trials
@@ -386,18 +391,6 @@ def run_spec_ours(args, rank, world, local_rank):
                                          C.c_void_p(rec.data_ptr()), sp)
         if st:
             raise cb.ComrsError(st, L.cb_link_last_error(link._h).decode())
-
-    def barrier():
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     for s in range(args.warmup):
         step(10_000 + s)
@@ -569,29 +562,12 @@ def run_mix_reference(args, rank):
 def run_mix_ours(args, rank, world, local_rank):
     import torch
 
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    dist, barrier, max_over_ranks = start_ranks(world, local_rank)
     cb = importlib.import_module("com-rs_gb300")
     items = cb.draw_mixed_batch(n=MIX_N, seed=MIX_ITEMS_SEED)
     mix = cb.MixBatch(items, seed=MIX_SEED, name=MIX_NAME, max_iterations=25, device=local_rank)
     tuned = cb.autotune(mix, reps=2, cache=False)
     bits = int(items["k_info"].sum())
-
-    def barrier():
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     for s in range(args.warmup):
         mix.run(epoch=10_000 + s)
@@ -707,12 +683,7 @@ def run_learned_reference(args, rank):
 def run_learned_ours(args, rank, world, local_rank):
     import torch
 
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    dist, barrier, max_over_ranks = start_ranks(world, local_rank)
     cb, Lm, p = learned_setup(args.protocol)
     B = LEARNED_FRAMES[args.protocol]
     pts = LEARNED_POINTS[args.protocol]
@@ -726,18 +697,6 @@ def run_learned_ours(args, rank, world, local_rank):
     Lm.load(net, os.path.join(ROOT, "com-rs_gb300", "weights", f"learned_{args.protocol}.npz"))
     decoders = {"learned": (net.run_frames, pts["learned"]), "plain_20": (nr(20).run_frames, pts["plain_20"]),
                 f"plain_{p['T']}": (nr(p["T"]).run_frames, pts["plain_T"])}
-
-    def barrier():
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     out, clocks_summary = {}, None
     for key, (run, eb) in decoders.items():
