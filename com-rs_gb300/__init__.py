@@ -80,6 +80,7 @@ SYMBOLS = [
     ("cb_nms_get_weights", _i32, [_vp, _vp, _vp]),
     ("cb_nms_set_weights", _i32, [_vp, _vp, _vp]),
     ("cb_nms_forward", _i32, [_vp, _vp, _i64, _vp]),
+    ("cb_nms_set_loss_bits", _i32, [_vp, _i32]),
     ("cb_nms_gradients", _i32, [_vp, _vp, _vp, _i64, _i32, _vp, _vp, C.POINTER(_dbl)]),
     ("cb_nms_train_step", _i32, [_vp, _i32, _u64, _u64, _i64, _dbl, _dbl, _dbl, _i32, C.POINTER(_dbl)]),
     ("cb_nms_decode", _i32, [_vp, _vp, _i64, _vp, _vp]),
@@ -351,6 +352,11 @@ class LearnedNms:
         its = np.zeros(x.shape[0], np.int32)
         _check(lib().cb_nms_decode(self._h, _p(x), x.shape[0], _p(post), _p(its)), self.code._h)
         return post, its
+
+    def set_loss_bits(self, info_only):
+        """The bits the training loss covers: all n_full codeword bits, or (info_only) the
+        K' information bits."""
+        _check(lib().cb_nms_set_loss_bits(self._h, int(bool(info_only))), self.code._h)
 
     def gradients(self, llr, cw, multi_loss=False):
         """(mean loss, d/d scales, d/d offsets) of frames of E LLRs against their n_full

@@ -599,6 +599,7 @@ cb_status cb_xoshiro_jump(const uint64_t state[4], uint64_t steps, uint64_t out[
 struct cb_nms {
   cb_code* code = nullptr;
   int T = 0, shared = 0, step = 0;
+  int info_only_loss = 0;  // 1: the loss covers the K' information bits only
   int64_t nw = 0;        // weights per kind (scales, offsets)
   float* d_w = nullptr;  // [2 nw]: scales then offsets
   float* d_g = nullptr;
@@ -715,6 +716,7 @@ cbk::LearnedArgs nms_args(cb_nms* h, int64_t n) {
   a.post_out = h->d_post;
   a.g_alpha = h->d_g;
   a.g_beta = h->d_g + h->nw;
+  a.loss_bits = h->info_only_loss ? h->code->host.k_info : h->code->host.n_full;
   return a;
 }
 
@@ -825,6 +827,12 @@ cb_status cb_nms_forward(cb_nms* h, const float* llr, int64_t n, float* post) {
   CB_CUDA(c, cbk::launch_learned(a, true, c->stream));
   CB_CUDA(c, cudaMemcpyAsync(post, h->d_post, (size_t)n * c->host.n_full * 4, cudaMemcpyDeviceToHost, c->stream));
   CB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CB_OK;
+}
+
+cb_status cb_nms_set_loss_bits(cb_nms* h, int32_t info_only) {
+  if (!h) return fail(nullptr, CB_ERR_CONFIG, "null learned decoder");
+  h->info_only_loss = info_only ? 1 : 0;
   return CB_OK;
 }
 

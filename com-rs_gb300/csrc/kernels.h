@@ -159,6 +159,7 @@ struct LearnedArgs {
   float* loss;              // sum over frames of the mean bit loss (training)
   float* P;                 // [n_frames][T][n_full] posteriors after each iteration (multi-loss)
   int32_t multi_loss;       // 0: last output; 1: every iteration's, 1/T each; 2: ramp 2(t+1)/(T(T+1))
+  int32_t loss_bits;        // the loss covers codeword bits [0, loss_bits): n_full, or K' (the information bits)
   float* g_alpha;           // gradients of the mean loss (backward)
   float* g_beta;
   const uint32_t* ref_bits;   // evaluation: sent info bits

@@ -10,8 +10,9 @@
 // lifted edge) or [t][entry] (one per base-graph edge, shared across Z); the edge
 // storage is [entry][r], so a layer's Z threads touch consecutive words.
 //
-// Training loss: the mean over frames and over the n_full codeword bits of
-// softplus(-(1 - 2 c_v) post_v), the binary cross-entropy of the soft output: of the
+// Training loss: the mean over frames and over the codeword bits [0, loss_bits) (all n_full
+// bits, or the K' information bits) of softplus(-(1 - 2 c_v) post_v), the binary
+// cross-entropy of the soft output: of the
 // last iteration, or (multi-loss) a weighted mean over the outputs of all T iterations,
 // whose posteriors the forward then saves: weights 1/T, or a ramp 2(t+1)/(T(T+1)).
 // Backward: for t = T-1..0 and the layers in reverse, each row recomputes its forward
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(384) learned_forward_kernel(const __grid_const
       if (multi) {
         const int wpc = (c.n_full + 31) >> 5;
         float* Pt = a.P + ((size_t)f * a.T + t) * c.n_full;
-        for (int v = tid; v < c.n_full; v += nt) {
+        for (int v = tid; v < a.loss_bits; v += nt) {
           Pt[v] = post[v];
           int bit = (a.cw_bits[(size_t)f * wpc + (v >> 5)] >> (v & 31)) & 1;
           lsum += softplus_f(bit ? post[v] : -post[v]) * iter_loss_weight(a.multi_loss, t, a.T);
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(384) learned_forward_kernel(const __grid_const
   if (a.cw_bits && a.loss) {
     if (!multi) {
       const int wpc = (c.n_full + 31) >> 5;
-      for (int v = tid; v < c.n_full; v += nt) {
+      for (int v = tid; v < a.loss_bits; v += nt) {
         int bit = (a.cw_bits[(size_t)f * wpc + (v >> 5)] >> (v & 31)) & 1;
         lsum += softplus_f(bit ? post[v] : -post[v]);
       }
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(384) learned_forward_kernel(const __grid_const
   if (be) atomicAdd(&s_err, be);
   __syncthreads();
   if (tid == 0) {
-    if (a.loss && a.cw_bits) atomicAdd(a.loss, s_loss / (float)c.n_full);
+    if (a.loss && a.cw_bits) atomicAdd(a.loss, s_loss / (float)a.loss_bits);
     if (a.iters_out) a.iters_out[f] = it;
     if (a.results) {
       cbd::FrameResult r;
@@ -318,7 +319,7 @@ __global__ void __launch_bounds__(384) learned_backward_kernel(const __grid_cons
   const float* X = a.X + (size_t)f * a.T * edges;
   const int wpc = (c.n_full + 31) >> 5;
   const bool multi = a.multi_loss && a.P;
-  const float scale = 1.f / ((float)c.n_full * (float)a.n_frames);
+  const float scale = 1.f / ((float)a.loss_bits * (float)a.n_frames);
   for (int v = tid; v < c.n_full; v += nt) gp[v] = 0.f;
   for (size_t i = tid; i < edges; i += nt) gc[i] = 0.f;
   if (tid < 38) red[tid] = 0.f;
@@ -329,7 +330,7 @@ __global__ void __launch_bounds__(384) learned_backward_kernel(const __grid_cons
     if (multi || t == a.T - 1) {
       const float* p = multi ? a.P + ((size_t)f * a.T + t) * c.n_full : a.post_out + (size_t)f * c.n_full;
       const float sc = multi ? scale * iter_loss_weight(a.multi_loss, t, a.T) : scale;
-      for (int v = tid; v < c.n_full; v += nt) {
+      for (int v = tid; v < a.loss_bits; v += nt) {
         int bit = (a.cw_bits[(size_t)f * wpc + (v >> 5)] >> (v & 31)) & 1;
         float sgn = bit ? -1.f : 1.f;
         gp[v] += -sgn * sigmoid_f(-sgn * p[v]) * sc;

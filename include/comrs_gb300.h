@@ -157,10 +157,13 @@ cb_status cb_nms_get_weights(cb_nms* nms, float* alpha, float* beta);
 cb_status cb_nms_set_weights(cb_nms* nms, const float* alpha, const float* beta);
 /* the n_full posteriors after exactly `iterations` iterations of n frames of E LLRs */
 cb_status cb_nms_forward(cb_nms* nms, const float* llr, int64_t n_frames, float* post);
+/* the bits the training loss covers: 0 all n_full codeword bits (the default), 1 the K'
+ * information bits (the bits whose errors the frame error rate counts) */
+cb_status cb_nms_set_loss_bits(cb_nms* nms, int32_t info_only);
 /* the mean loss (binary cross-entropy of the soft output against the n_full codeword
- * bytes `cw`; multi_loss 0: of the last output, 1: the mean over the outputs of all T
- * iterations, 2: their weighted mean with weights 2 (t + 1) / (T (T + 1)), t = 0..T-1)
- * of n frames and its gradients (nullable outputs) */
+ * bytes `cw`, over the bits of cb_nms_set_loss_bits; multi_loss 0: of the last output,
+ * 1: the mean over the outputs of all T iterations, 2: their weighted mean with weights
+ * 2 (t + 1) / (T (T + 1)), t = 0..T-1) of n frames and its gradients (nullable outputs) */
 cb_status cb_nms_gradients(cb_nms* nms, const float* llr, const uint8_t* cw, int64_t n_frames, int32_t multi_loss,
                            float* g_alpha, float* g_beta, double* loss);
 /* one Adam step (learning rate lr) on `batch` frames drawn by the frame generator at

@@ -866,7 +866,8 @@ static LinkCounts link_trial(const Code& c, const Qam& q, const GridSlicer& g, i
 //   y_e = s_e * max(alpha[t, e] * m_e - beta[t, e], 0)
 // (s_e the sign product and m_e the minimum magnitude over the row's other edges, as
 // check_message, ldpc.rs:468-491), run for exactly T iterations, and its loss
-//   L = sum over the frame's n_full bits of softplus(-(1 - 2 c_v) post_v) / n_full
+//   L = sum over the frame's bits [0, loss_bits) (n_full, or K') of
+//       softplus(-(1 - 2 c_v) post_v) / loss_bits
 // with the gradient of L with respect to every alpha and beta by reverse-mode
 // differentiation of the T unrolled iterations (the minimum is differentiated
 // through its argmin; sign and max(., 0) through their derivatives almost everywhere).
@@ -878,6 +879,7 @@ struct Learned {
   bool shared;
   std::vector<int> lstart;  // base row -> first entry
   int multi = 0;  // 0: the last output's loss; 1: every iteration's, 1/T each; 2: ramp 2(t+1)/(T(T+1))
+  int loss_bits = 0;  // the loss covers codeword bits [0, loss_bits): n_full, or K'
 };
 
 static void learned_layers(const Code& c, std::vector<int>& lstart) {
@@ -932,8 +934,8 @@ static double learned_frame(const Learned& L, const double* full_llr, const uint
   }
   auto bit_loss = [&](const double* p) {
     double l = 0.0;
-    for (int v = 0; v < c.n; v++) l += softplus(-(1.0 - 2.0 * cw[v]) * p[v]);
-    return l / (double)c.n;
+    for (int v = 0; v < L.loss_bits; v++) l += softplus(-(1.0 - 2.0 * cw[v]) * p[v]);
+    return l / (double)L.loss_bits;
   };
   double loss = 0.0;
   auto weight = [&](int t) { return L.multi == 2 ? 2.0 * (t + 1) / ((double)T * (T + 1)) : 1.0 / (double)T; };
@@ -946,9 +948,9 @@ static double learned_frame(const Learned& L, const double* full_llr, const uint
   // reverse sweep
   std::vector<double> gp(c.n, 0.0), gc(edges, 0.0);
   auto add_loss_grad = [&](const double* p, double w) {
-    for (int v = 0; v < c.n; v++) {
+    for (int v = 0; v < L.loss_bits; v++) {
       double sgn = 1.0 - 2.0 * cw[v];
-      gp[v] += -sgn * sigmoid(-sgn * p[v]) * w / (double)c.n;
+      gp[v] += -sgn * sigmoid(-sgn * p[v]) * w / (double)L.loss_bits;
     }
   };
   std::vector<double> gabs(32), gy(32);
@@ -1228,9 +1230,9 @@ void or_bpsk_llr_batch(void* h, uint64_t seed, uint64_t name_hash, uint64_t cond
 // accumulated) of `n` frames of e received LLRs and n_full codeword bits; returns the
 // mean loss over the frames
 double or_learned(void* h, int T, int shared, int multi, const double* alpha, const double* beta, const double* llr,
-                  const uint8_t* cw, int64_t n, double* post_out, double* ga, double* gb) {
+                  const uint8_t* cw, int64_t n, double* post_out, double* ga, double* gb, int info_only) {
   Code* c = (Code*)h;
-  Learned L{c, T, shared != 0, {}, multi};
+  Learned L{c, T, shared != 0, {}, multi, info_only ? c->k_info : c->n};
   learned_layers(*c, L.lstart);
   std::vector<double> full(c->n);
   double tot = 0.0;

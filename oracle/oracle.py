@@ -78,7 +78,7 @@ def lib():
         L.or_run_frames.restype = i32
         L.or_run_frames.argtypes = [vp, i32, u64, u64, u64, u64, u64, dbl, i32, i32, i32, vp]
         L.or_learned.restype = dbl
-        L.or_learned.argtypes = [vp, i32, i32, i32, vp, vp, vp, vp, i64, vp, vp, vp]
+        L.or_learned.argtypes = [vp, i32, i32, i32, vp, vp, vp, vp, i64, vp, vp, vp, i32]
         L.or_learned_num_weights.restype = i64
         L.or_learned_num_weights.argtypes = [vp, i32, i32]
         L.or_bpsk_frame.restype = i32
@@ -261,8 +261,10 @@ class Code:
             raise ValueError("bad modulation")
         return out
 
-    def learned(self, T, shared, alpha, beta, llr, cw, want_post=False, want_grad=False, multi=False):
-        """(mean loss, post [n x n_full] or None, (d alpha, d beta) or None) of the learned min-sum."""
+    def learned(self, T, shared, alpha, beta, llr, cw, want_post=False, want_grad=False, multi=False,
+                info_only=False):
+        """(mean loss, post [n x n_full] or None, (d alpha, d beta) or None) of the learned min-sum;
+        info_only: the loss over the K' information bits instead of all n_full bits."""
         llr = np.ascontiguousarray(llr, np.float64).reshape(-1, self.e)
         cw = np.ascontiguousarray(cw, np.uint8).reshape(-1, self.n_full)
         n = llr.shape[0]
@@ -272,7 +274,7 @@ class Code:
         ga = np.zeros_like(alpha) if want_grad else None
         gb = np.zeros_like(beta) if want_grad else None
         loss = lib().or_learned(self.h, T, int(shared), int(multi), _p(alpha), _p(beta), _p(llr), _p(cw), n, _p(post), _p(ga),
-                                _p(gb))
+                                _p(gb), int(bool(info_only)))
         return loss, post, (None if ga is None else (ga / n, gb / n))
 
     def learned_num_weights(self, T, shared):

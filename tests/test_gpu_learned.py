@@ -39,12 +39,15 @@ def test_plain_weights_forward_is_the_min_sum(cb, O, shared):
     assert compared >= 10
 
 
-@pytest.mark.parametrize("shared,multi", [(False, 0), (True, 0), (False, 1), (True, 1), (False, 2), (True, 2)])
-def test_gradients_match_the_f64_oracle(cb, O, shared, multi):
+@pytest.mark.parametrize("shared,multi,info_only", [(False, 0, False), (True, 0, False), (False, 1, False),
+                                                     (True, 1, False), (False, 2, False), (True, 2, False),
+                                                     (True, 1, True), (False, 0, True)])
+def test_gradients_match_the_f64_oracle(cb, O, shared, multi, info_only):
     T = 5
     g = cb.NrLdpc(100, 300, base_graph=2, lifting_size=10, precision="f32")
     ref = O.Code(100, 300, bg=2, z=10)
     net = cb.LearnedNms(g, T, shared=shared)
+    net.set_loss_bits(info_only)
     rng = np.random.default_rng(2)
     alpha = (0.75 + 0.05 * rng.standard_normal(net.n_weights)).astype(np.float32)
     beta = (0.05 * np.abs(rng.standard_normal(net.n_weights))).astype(np.float32)
@@ -52,7 +55,7 @@ def test_gradients_match_the_f64_oracle(cb, O, shared, multi):
     llr, cw = oracle_frames(O, ref, 16, 1.0)
     loss, ga, gb = net.gradients(llr, cw, multi_loss=multi)
     rloss, _, (rga, rgb) = ref.learned(T, shared, alpha.astype(np.float64), beta.astype(np.float64),
-                                       llr.astype(np.float64), cw, want_grad=True, multi=multi)
+                                       llr.astype(np.float64), cw, want_grad=True, multi=multi, info_only=info_only)
     assert abs(loss - rloss) <= 1e-4 * abs(rloss)
     for got, want in ((ga, rga), (gb, rgb)):
         cos = float(got @ want / (np.linalg.norm(got) * np.linalg.norm(want)))

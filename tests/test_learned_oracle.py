@@ -37,8 +37,9 @@ def test_plain_weights_are_the_min_sum(O, shared):
     assert compared >= 3
 
 
-@pytest.mark.parametrize("shared,multi", [(False, 0), (True, 0), (False, 1), (True, 2)])
-def test_gradients_match_finite_differences(O, shared, multi):
+@pytest.mark.parametrize("shared,multi,info_only", [(False, 0, False), (True, 0, False), (False, 1, False),
+                                                     (True, 2, False), (True, 1, True), (False, 0, True)])
+def test_gradients_match_finite_differences(O, shared, multi, info_only):
     code = O.Code(40, 80, bg=2, z=4)  # a small lifted code
     T = 4
     nw = code.learned_num_weights(T, shared)
@@ -46,16 +47,16 @@ def test_gradients_match_finite_differences(O, shared, multi):
     alpha = 0.75 + 0.1 * rng.standard_normal(nw)
     beta = 0.05 * np.abs(rng.standard_normal(nw))
     llr, cw = frames(O, code, 3, 1.0)
-    loss, _, (ga, gb) = code.learned(T, shared, alpha, beta, llr, cw, want_grad=True, multi=multi)
+    loss, _, (ga, gb) = code.learned(T, shared, alpha, beta, llr, cw, want_grad=True, multi=multi, info_only=info_only)
     h = 1e-6
     idx = rng.choice(nw, 12, replace=False)
     for i in idx:
         for w, g in ((alpha, ga), (beta, gb)):
             w0 = w[i]
             w[i] = w0 + h
-            lp, _, _ = code.learned(T, shared, alpha, beta, llr, cw, multi=multi)
+            lp, _, _ = code.learned(T, shared, alpha, beta, llr, cw, multi=multi, info_only=info_only)
             w[i] = w0 - h
-            lm, _, _ = code.learned(T, shared, alpha, beta, llr, cw, multi=multi)
+            lm, _, _ = code.learned(T, shared, alpha, beta, llr, cw, multi=multi, info_only=info_only)
             w[i] = w0
             fd = (lp - lm) / (2 * h)
             assert abs(fd - g[i]) <= 1e-6 + 1e-4 * abs(fd), (i, fd, g[i])
