@@ -610,7 +610,7 @@ def run_mix_ours(args, rank, world, local_rank):
                            "rows_per_thread": {str(z): v[0] for z, v in tuned.items()},
                            "timing": "host clock around the synchronous replay call (device work and the 128 KB "
                                      "of records); value and e2e are the same measurement",
-                           "l2": "each replay writes and reads its LLRs once; no flush between replays",
+                           "l2": f"inputs larger than L2: each replay writes and reads {algo / 1e6:.0f} MB of LLRs",
                            "parallelism": f"dp{world} (disjoint epochs per GPU)",
                            "mean_fer": float(np.mean(fer))},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
@@ -739,6 +739,8 @@ def run_learned_ours(args, rank, world, local_rank):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (Monte Carlo frames from seeded streams)",
                 "config": {"workload": learned_workload(p, args.protocol), "frames_per_step": B,
+                           "l2": f"inputs larger than L2: each step writes and reads {B * p['e'] * 4 / 1e6:.0f} MB "
+                                 f"of LLRs",
                            "decoders": out, "timing": "host clock around cb_nms_run_frames / cb_run_frames "
                                                        "(generation, decoding, records to the host)",
                            "parallelism": f"dp{world} (disjoint frame ranges per GPU)"},
