@@ -405,6 +405,8 @@ def _link_settings(link):
         raise ValueError("link: the GPU runs fec_encode, map, awgn_ebn0, demap, fec_decode, got "
                          f"{[k for k, _ in kinds]}")
     enc, mp, awgn, dm, dec = (p for _, p in kinds)
+    if awgn.get("ebn0_db") is None:
+        raise ValueError("awgn_ebn0: ebn0_db is required")
     code, dcode = enc.get("code"), dec.get("code")
     for c in (code, dcode):
         if not isinstance(c, dict) or c.get("type") != "ldpc":

@@ -106,6 +106,10 @@ def test_link_settings(cb):
         spec._link_settings(bad)
     with pytest.raises(ValueError, match="the GPU runs"):
         spec._link_settings(BICM_LDPC["link"][:3])
+    bad = [dict(b) if isinstance(b, dict) else b for b in BICM_LDPC["link"]]
+    bad[2] = {"type": "awgn_ebn0"}
+    with pytest.raises(ValueError, match="ebn0_db is required"):
+        spec._link_settings(bad)
 
 
 def test_link_host_tables(cb, O):
