@@ -240,7 +240,9 @@ cb_status cb_ldpc_levels(const cb_ldpc* code, int32_t* level_start, int32_t* lev
  * posteriors of every frame into `post` and the iterations used into `iterations`
  * (both host, nullable) */
 cb_status cb_ldpc_decode(cb_ldpc* code, const void* llr, int64_t n_frames, void* post, int32_t* iterations);
-/* the same on device buffers, enqueued on `stream` (cudaStream_t, NULL = default) */
+/* the same on device buffers, enqueued on `stream` (cudaStream_t, NULL = default).  The
+ * decodes of one code object share its work counter and message slots: enqueue them on
+ * one stream, or let each finish before the next starts on another. */
 cb_status cb_ldpc_decode_device(cb_ldpc* code, const void* llr_dev, int64_t n_frames, void* post_dev,
                                 int32_t* iterations_dev, void* stream);
 /* LdpcCode::set_decoder (bindings/com-py/src/fec/ldpc_code.rs:74-86): new decoder
@@ -316,7 +318,8 @@ cb_status cb_link_run_trials(cb_link* link, uint64_t seed, uint64_t name_hash, u
                              uint64_t first_trial, int64_t n_trials, double ebn0_db, cb_link_record* out);
 /* cb_link_run_trials enqueued on `stream` (cudaStream_t, NULL = default) with the records in
  * device memory; the link's scratch holds at most 1 GB of trials per call (CB_ERR_SHAPE
- * beyond).  Asynchronous: the caller synchronises its stream. */
+ * beyond).  Asynchronous: the caller synchronises its stream.  It decodes with the code
+ * object's scratch, so the rule of cb_ldpc_decode_device applies to the two together. */
 cb_status cb_link_run_trials_device(cb_link* link, uint64_t seed, uint64_t name_hash, uint64_t condition,
                                     uint64_t first_trial, int64_t n_trials, double ebn0_db, cb_link_record* out_dev,
                                     void* stream);
