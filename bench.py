@@ -498,6 +498,9 @@ def run_spec_ours(args, rank, world, local_rank):
 
 
 MIX_N, MIX_ITEMS_SEED, MIX_SEED, MIX_NAME = 16384, 2024, 7, "bicm_ldpc_mix"
+# dram__bytes_read.sum + dram__bytes_write.sum of the decode phase of one replay
+# (profiles/mix_decode.md: 290,330,880 + 17,780,224 B)
+MIX_TRAFFIC = 290_330_880 + 17_780_224
 MIX_METRIC = "decoded info Gbit/s of the uneven mixed batch (one graph replay per step); vs CPU Runner"
 MIX_WORKLOAD = ("16,384 codewords per replay, each: BG {1,2}, Z {16,32,64,128,208,384}, R {1/3,1/2,2/3,5/6}, "
                 "Gray QPSK..256-QAM, Eb/N0 U[0,6] dB (item seed 2024); f32, layered NMS alpha=0.75, <=25 "
@@ -588,7 +591,9 @@ def run_mix_ours(args, rank, world, local_rank):
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = algo / (dec_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "mix_decode_kernel (decode phase of a replay)",
+                "traffic": MIX_TRAFFIC, "traffic_source": "ncu capture of the decode phase of one replay of this "
+                                                          "batch (bench.py --workload mix --profile-case)",
+                "kernel": "mix_decode_kernel (decode phase of a replay)",
                 "algorithmic_bytes_per_launch": algo, "launch_ms": dec_ms,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
                 "note": "issue-bound like the single-code decoder; the HBM fraction is the algorithmic-bytes one"}
@@ -626,6 +631,9 @@ def run_mix_ours(args, rank, world, local_rank):
 LEARNED_POINTS = {"c5": {"learned": 6.97, "plain_20": 6.51, "plain_T": 7.33},
                   "c4": {"learned": 2.17, "plain_20": 2.09, "plain_T": 2.35}}
 LEARNED_FRAMES = {"c5": 8192, "c4": 65536}
+# dram__bytes_read.sum + dram__bytes_write.sum of one decode of a step's frames
+# (profiles/learned_decode_c5.md: 554,730,752 + 16,534,016 B)
+LEARNED_TRAFFIC = {"c5": 554_730_752 + 16_534_016}
 LEARNED_METRIC = "decoded info Gbit/s at equal FER (1e-3), neural vs plain min-sum; vs CPU Runner"
 
 
@@ -718,15 +726,44 @@ def run_learned_ours(args, rank, world, local_rank):
         if key == "learned":
             clocks_summary = clocks.summary()
     lv = out["learned"]
+    # roofline of the learned decoder kernel: one step's frames generated into HBM, then
+    # cb_nms_decode_device timed with CUDA events on torch's stream (the LLRs exceed L2)
+    llr = torch.empty((B, p["e"]), dtype=torch.float32, device=f"cuda:{local_rank}")
+    info = torch.empty((B, (p["k"] + 31) // 32), dtype=torch.int32, device=f"cuda:{local_rank}")
+    post = torch.empty((B, code.n_full), dtype=torch.float32, device=f"cuda:{local_rank}")
+    its = torch.empty(B, dtype=torch.int32, device=f"cuda:{local_rank}")
+    sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    L = cb.lib()
+    st = L.cb_generate_frames_device(code._h, p["m"], 3, cb.fnv1a64("learned_bench"), 0, 0, B, pts["learned"],
+                                     C.c_void_p(llr.data_ptr()), C.c_void_p(info.data_ptr()), sp)
+    dec = []
+    for rep in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        st |= L.cb_nms_decode_device(net._h, C.c_void_p(llr.data_ptr()), B, C.c_void_p(post.data_ptr()),
+                                     C.c_void_p(its.data_ptr()), sp)
+        e1.record()
+        torch.cuda.synchronize()
+        if rep:
+            dec.append(e0.elapsed_time(e1))
+    if st:
+        raise cb.ComrsError(st, L.cb_last_error(code._h).decode())
+    dec_ms = float(np.mean(dec))
     algo = B * (p["e"] * 4 + (p["k"] + 7) // 8 + 4)
     peaks = read_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
-    achieved = algo / (lv["ms_per_step"] * 1e-3) / 1e9
+    achieved = algo / (dec_ms * 1e-3) / 1e9
+    traffic = LEARNED_TRAFFIC.get(args.protocol)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "layered learned decoder, timed with the frame generator (one step)",
-                "algorithmic_bytes_per_launch": algo, "launch_ms": lv["ms_per_step"],
+                "traffic": traffic,
+                "traffic_source": "ncu capture of one decode of this step's frames (bench.py --workload learned "
+                                  "--profile-case)" if traffic else None,
+                "kernel": "layered decoder with the learned weights (cb_nms_decode_device)",
+                "algorithmic_bytes_per_launch": algo, "launch_ms": dec_ms,
+                "launch_mean_iterations": float(its.float().mean()),
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
-                "note": "issue-bound like the plain decoder; the step includes the generator"}
+                "note": "issue-bound like the plain decoder; algorithmic bytes: E LLRs in, K' decided bits and "
+                        "the iteration count out per frame"}
     cpu = None
     if rank == 0 and not args.no_cpu:
         gbps, cores, n, t, fer = learned_cpu_sample(args.protocol, 5.0)
@@ -747,7 +784,7 @@ def run_learned_ours(args, rank, world, local_rank):
                 "e2e": {"value": lv["value"], "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": B * 8,
                         "api": "cb_nms_run_frames (records to the host)"},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks_summary,
-                "gpu_launches": 2 * args.steps}
+                "gpu_launches": 2 * -(-B // 16384) * args.steps}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -808,6 +845,45 @@ def run_profile_case(args):
     print(json.dumps({"profile_case": n, "mean_iterations": float(iters.float().mean())}))
 
 
+def run_mix_profile_case(args):
+    """The small case of the mixed batch for ncu: the bench's batch, rows per thread at
+    their defaults, replayed three times (generator and decoder each time)."""
+    cb = importlib.import_module("com-rs_gb300")
+    items = cb.draw_mixed_batch(n=MIX_N, seed=MIX_ITEMS_SEED)
+    mix = cb.MixBatch(items, seed=MIX_SEED, name=MIX_NAME, max_iterations=25, device=0)
+    fer = [float(mix.run(epoch=s)["frame_error"].mean()) for s in range(3)]
+    mix.close()
+    print(json.dumps({"profile_case": "mix", "items": MIX_N, "fer": fer}))
+
+
+def run_learned_profile_case(args):
+    """The small case of the learned decoder for ncu: one step's frames of the protocol
+    generated at the learned decoder's FER 1e-3 point, then decoded three times."""
+    import torch
+
+    cb, Lm, p = learned_setup(args.protocol)
+    B = LEARNED_FRAMES[args.protocol]
+    code = cb.NrLdpc(p["k"], p["e"], base_graph=p["bg"], lifting_size=p["z"], precision="f32",
+                     max_iterations=p["T"])
+    net = cb.LearnedNms(code, p["T"], shared=p["shared"])
+    Lm.load(net, os.path.join(ROOT, "com-rs_gb300", "weights", f"learned_{args.protocol}.npz"))
+    llr = torch.empty((B, p["e"]), dtype=torch.float32, device="cuda")
+    info = torch.empty((B, (p["k"] + 31) // 32), dtype=torch.int32, device="cuda")
+    its = torch.empty(B, dtype=torch.int32, device="cuda")
+    sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    L = cb.lib()
+    st = L.cb_generate_frames_device(code._h, p["m"], 3, cb.fnv1a64("learned_bench"), 0, 0, B,
+                                     LEARNED_POINTS[args.protocol]["learned"], C.c_void_p(llr.data_ptr()),
+                                     C.c_void_p(info.data_ptr()), sp)
+    for _ in range(3):
+        st |= L.cb_nms_decode_device(net._h, C.c_void_p(llr.data_ptr()), B, None, C.c_void_p(its.data_ptr()), sp)
+    torch.cuda.synchronize()
+    if st:
+        raise cb.ComrsError(st, L.cb_last_error(code._h).decode())
+    print(json.dumps({"profile_case": "learned", "protocol": args.protocol, "frames": B,
+                      "mean_iterations": float(its.float().mean())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -822,14 +898,12 @@ def main():
     ap.add_argument("--protocol", choices=["c5", "c4"], default="c5", help="the code of --workload learned")
     ap.add_argument("--trials", type=int, default=2048, help="trials per step of --workload spec")
     ap.add_argument("--profile-case", action="store_true",
-                    help="generate --frames C2 codewords (--workload spec: --trials trials) and decode them "
-                         "three times (for ncu)")
+                    help="generate --frames C2 codewords (--workload spec: --trials trials; mix: the batch; "
+                         "learned: one step's frames) and decode them three times (for ncu)")
     args = ap.parse_args()
     if args.profile_case:
-        if args.workload == "spec":
-            run_spec_profile_case(args)
-        else:
-            run_profile_case(args)
+        {"spec": run_spec_profile_case, "mix": run_mix_profile_case, "learned": run_learned_profile_case,
+         "c2": run_profile_case}[args.workload](args)
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -84,6 +84,7 @@ SYMBOLS = [
     ("cb_nms_gradients", _i32, [_vp, _vp, _vp, _i64, _i32, _vp, _vp, C.POINTER(_dbl)]),
     ("cb_nms_train_step", _i32, [_vp, _i32, _u64, _u64, _i64, _dbl, _dbl, _dbl, _i32, C.POINTER(_dbl)]),
     ("cb_nms_decode", _i32, [_vp, _vp, _i64, _vp, _vp]),
+    ("cb_nms_decode_device", _i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
     ("cb_nms_run_frames", _i32, [_vp, _i32, _u64, _u64, _u64, _u64, _i64, _dbl, _vp]),
     ("cb_mix_create", _i32, [_vp, _i64, _u64, _u64, _dbl, _i32, _i32, C.POINTER(_vp)]),
     ("cb_mix_destroy", None, [_vp]),

@@ -921,6 +921,20 @@ cb_status cb_nms_decode(cb_nms* h, const float* llr, int64_t n, float* post, int
   return CB_OK;
 }
 
+cb_status cb_nms_decode_device(cb_nms* h, const float* llr, int64_t n, float* post, int32_t* iterations,
+                               void* stream) {
+  if (!h || (!llr && n > 0) || n < 0) return fail(nullptr, CB_ERR_CONFIG, "NULL argument or negative count");
+  cb_code* c = h->code;
+  std::lock_guard<std::mutex> lock(c->mu);
+  CB_CUDA(c, cudaSetDevice(c->device));
+  if (n == 0) return CB_OK;
+  std::vector<float> pw;
+  bool in_params = false;
+  if (cb_status st = nms_param_weights(h, pw, in_params)) return st;
+  // the persistent decoder takes any number of frames; its per-CTA state is the code's
+  return nms_eval(h, llr, n, nullptr, nullptr, post, iterations, (cudaStream_t)stream, in_params ? &pw : nullptr);
+}
+
 cb_status cb_nms_run_frames(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_hash, uint64_t cond, uint64_t first,
                             int64_t n, double ebn0_db, cb_frame_result* out) {
   if (!h || !out || n < 0) return fail(nullptr, CB_ERR_CONFIG, "NULL argument or negative count");

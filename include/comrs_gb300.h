@@ -107,7 +107,9 @@ cb_status cb_decode(cb_code* code, const void* llr, int64_t n_frames, uint8_t* b
                     int32_t* iterations);
 
 /* cb_decode on device buffers and a caller stream (cudaStream_t, NULL = default):
- * bits: n_frames x ceil(K'/32) uint32 words, packed LSB first. */
+ * bits: n_frames x ceil(K'/32) uint32 words, packed LSB first.  The device calls of one
+ * code object share its work counter and per-CTA state: enqueue them on one stream, or
+ * let each finish before the next starts on another. */
 cb_status cb_decode_device(cb_code* code, const void* llr_dev, int64_t n_frames, uint32_t* bits_dev,
                            void* app_dev, int32_t* iterations_dev, void* stream);
 
@@ -177,6 +179,10 @@ cb_status cb_nms_train_step(cb_nms* nms, int32_t modulation_order, uint64_t seed
  * Runs the layered decoder with the network's weights (the same results as the
  * training forward, which runs all iterations) */
 cb_status cb_nms_decode(cb_nms* nms, const float* llr, int64_t n_frames, float* post, int32_t* iterations);
+/* the same on device buffers, enqueued on `stream` (cudaStream_t, NULL = default); it
+ * runs on the code object's scratch, so the ordering rule of cb_decode_device holds */
+cb_status cb_nms_decode_device(cb_nms* nms, const float* llr_dev, int64_t n_frames, float* post_dev,
+                               int32_t* iterations_dev, void* stream);
 /* cb_run_frames with the learned decoder (syndrome stop after each iteration) */
 cb_status cb_nms_run_frames(cb_nms* nms, int32_t modulation_order, uint64_t seed, uint64_t name_hash,
                             uint64_t condition, uint64_t first_frame, int64_t n_frames, double ebn0_db,

@@ -102,6 +102,19 @@ def test_fast_evaluation_equals_the_training_forward(cb, O, shared, k, e, z):
     assert np.array_equal(post[ran_all].view(np.uint32), full[ran_all].view(np.uint32))
     for f in np.flatnonzero(~ran_all):
         assert ref.is_codeword((post[f] < 0).astype(np.uint8))
+    # on device buffers and a caller stream: the same posteriors and iterations
+    import ctypes as C
+    import torch
+    d_llr = torch.from_numpy(llr).cuda()
+    d_post = torch.zeros((llr.shape[0], g.n_full), dtype=torch.float32, device="cuda")
+    d_its = torch.zeros(llr.shape[0], dtype=torch.int32, device="cuda")
+    st = cb.lib().cb_nms_decode_device(net._h, C.c_void_p(d_llr.data_ptr()), llr.shape[0],
+                                       C.c_void_p(d_post.data_ptr()), C.c_void_p(d_its.data_ptr()),
+                                       C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    assert st == 0
+    assert np.array_equal(d_its.cpu().numpy(), its)
+    assert np.array_equal(d_post.cpu().numpy().view(np.uint32), post.view(np.uint32))
     # the Monte Carlo records come from the same path
     rec = net.run_frames(5, NAME, 0, 0, 64, 1.0, 4)
     llr2, info2 = g.generate_frames(5, NAME, 0, 0, 64, 1.0, 4)
