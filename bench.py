@@ -452,7 +452,8 @@ def run_spec_ours(args, rank, world, local_rank):
     peaks = read_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "sparse_kernel<double, sum-product, layered> (generic decoder)",
+                "traffic": None, "kernel": "sparse_group_kernel<double, sum-product, register rows> (generic decoder, several codewords "
+                          "per CTA)",
                 "algorithmic_bytes_per_launch": T * SPEC_BLOCKS * SPEC_ALGO_BYTES, "launch_ms": dec,
                 "mean_iterations": float(iters.float().mean()),
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",

@@ -18,17 +18,19 @@
 //
 // Every step is an explicitly rounded IEEE operation in the reference's order.  The
 // min-sum rules are therefore bit-exact in f64 (and equal to the same algorithm in f32).
-// The sum-product rule calls CUDA's tanh and atanh where the reference calls the
-// platform libm: results agree to rounding, not bit for bit.
+// The sum-product rule calls CUDA's tanh where the reference calls the platform libm,
+// and in f64 computes 2 atanh with atanh2.cuh (in f32 CUDA's atanhf): results agree to
+// rounding, not bit for bit.
 #include <cuda_runtime.h>
 
+#include "atanh2.cuh"
 #include "decode_common.cuh"
 #include "kernels.h"
 
 namespace cbk {
 namespace {
 
-// TANH_BOUND of ldpc.rs:37; it rounds to 1 in f32, where the bound is the largest
+// TANH_BOUND of ldpc.rs:93; it rounds to 1 in f32, where the bound is the largest
 // float below 1 (1 - 2^-24)
 template <typename T>
 __device__ __forceinline__ T tanh_bound();
@@ -39,13 +41,17 @@ __device__ __forceinline__ float tanh_bound<float>() { return __uint_as_float(0x
 
 __device__ __forceinline__ double tanh_t(double x) { return tanh(x); }
 __device__ __forceinline__ float tanh_t(float x) { return tanhf(x); }
-__device__ __forceinline__ double atanh_t(double x) { return atanh(x); }
-__device__ __forceinline__ float atanh_t(float x) { return atanhf(x); }
 
 // f64::clamp(lo, hi)
 template <typename T>
 __device__ __forceinline__ T clamp_t(T x, T lo, T hi) {
   return x < lo ? lo : (x > hi ? hi : x);
+}
+
+// the check-node output 2 atanh(clamp(p, -TANH_BOUND, TANH_BOUND)) (ldpc.rs:451-466)
+__device__ __forceinline__ double twice_atanh_t(double p) { return at2::twice_atanh(p, tanh_bound<double>()); }
+__device__ __forceinline__ float twice_atanh_t(float p) {
+  return mul_rn(2.0f, atanhf(clamp_t(p, -tanh_bound<float>(), tanh_bound<float>())));
 }
 
 // One check node.  The incoming message of edge i is post - c2v.  Layered: the outputs
@@ -86,7 +92,7 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, int pos, 
       const T t = msg[e];
       const T p = mul_rn(aux[e], suffix);
       suffix = mul_rn(suffix, t);
-      const T o = mul_rn((T)2, atanh_t(clamp_t(p, -tanh_bound<T>(), tanh_bound<T>())));
+      const T o = twice_atanh_t(p);
       if (LAYERED) {
         msg[e] = o;
         post[v] = add_rn(post[v], o);
@@ -151,7 +157,7 @@ __device__ __forceinline__ void check_row_spa_regs(const SparseDev& c, int row, 
     if (k < d) {
       const T p = mul_rn(pre[k], suffix);
       suffix = mul_rn(suffix, t[k]);
-      const T o = mul_rn((T)2, atanh_t(clamp_t(p, -tanh_bound<T>(), tanh_bound<T>())));
+      const T o = twice_atanh_t(p);
       msg[es.slot(k)] = o;
       post[es.var(k)] = add_rn(l[k], o);
     }
@@ -217,7 +223,7 @@ __device__ __forceinline__ void check_row_warp(const SparseDev& c, int row, T* p
       scarry = mul_rn(scarry, __shfl_sync(0xffffffffu, inc, 0));
       if (e < e1) {
         const T p = mul_rn(pre_r[k], suf);
-        const T o = mul_rn((T)2, atanh_t(clamp_t(p, -tanh_bound<T>(), tanh_bound<T>())));
+        const T o = twice_atanh_t(p);
         msg[e] = o;
         post[c.vars[e]] = add_rn(l_r[k], o);
       }
