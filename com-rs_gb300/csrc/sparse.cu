@@ -384,8 +384,10 @@ __device__ __forceinline__ void group_syndrome(const SparseDev& c, const T* base
   }
 }
 
+// two CTAs of up to 512 threads fit an SM in f32 (at most 64 registers); one in f64, whose
+// rows need more (without the bound the compiler held the f64 min-sum rows to 40 and spilled)
 template <typename T, int RULE, bool REGS>
-__global__ void __launch_bounds__(512) sparse_group_kernel(const __grid_constant__ SparseArgs<T> a) {
+__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1) sparse_group_kernel(const __grid_constant__ SparseArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SparseDev& c = a.code;
   const int tid = threadIdx.x, nt = blockDim.x, G = a.group;
