@@ -7,7 +7,7 @@
 //   * 1 + a and 1 - a are exact double-double sums; u = q + ul is their quotient to about
 //     2^-100 relative: q = s RN(1/d), and the remainder by fused multiply-adds.
 //   * log u by Tang's table-driven method (P. T. P. Tang, ACM TOMS 16(4), 1990), tables
-//     in atanh2_table.inc.  q = 2^e m with m in [1, 2); j = round(256 (m - 1)); r = m c_j - 1,
+//     in logtab.inc.  q = 2^e m with m in [1, 2); j = round(256 (m - 1)); r = m c_j - 1,
 //     exact; log u = e ln 2 - ln c_j + log1p(r) + ul / q, with log1p(r) = r + r^2 Q(r) from
 //     its Taylor series (|r| < 2^-8, truncation below 2^-61 relative), ln 2 and ln c_j as
 //     hi + lo pairs whose hi parts add exactly, and ul / q = ul c_j 2^-e (1 - r) to first
@@ -30,15 +30,9 @@
 #define AT2_HD inline
 #endif
 
-#if defined(__CUDA_ARCH__)
-#define ATANH2_CONST __device__ static const
-#else
-#define ATANH2_CONST static const
-#endif
-
 #include <cstring>
 
-#include "atanh2_table.inc"
+#include "logtab.inc"
 
 namespace at2 {
 
@@ -50,7 +44,7 @@ __device__ __forceinline__ double fma_rn(double a, double b, double c) { return 
 __device__ __forceinline__ double rcp(double a) { return __drcp_rn(a); }
 __device__ __forceinline__ uint64_t bits(double x) { return (uint64_t)__double_as_longlong(x); }
 __device__ __forceinline__ double from_bits(uint64_t b) { return __longlong_as_double((long long)b); }
-__device__ __forceinline__ double tab(int j, int k) { return __ldg(&ATANH2_TAB[j][k]); }
+__device__ __forceinline__ double tab(int j, int k) { return __ldg(&LOGTAB[j][k]); }
 #else
 inline double add(double a, double b) { return a + b; }
 inline double sub(double a, double b) { return a - b; }
@@ -67,7 +61,7 @@ inline double from_bits(uint64_t b) {
   std::memcpy(&x, &b, 8);
   return x;
 }
-inline double tab(int j, int k) { return ATANH2_TAB[j][k]; }
+inline double tab(int j, int k) { return LOGTAB[j][k]; }
 #endif
 
 // 2 atanh(clamp(p, -bound, bound)) (see the header comment for the domain)
@@ -101,12 +95,12 @@ AT2_HD double twice_atanh(double p, double bound) {
   const double cs = from_bits(bits(c) - ((uint64_t)e << 52));
   const double d0 = mul(ul, cs);
   const double delta = fma_rn(-d0, r, d0);
-  double qp = ATANH2_Q[ATANH2_Q_TERMS - 1];
-  for (int k = ATANH2_Q_TERMS - 2; k >= 0; k--) qp = fma_rn(qp, r, ATANH2_Q[k]);
+  double qp = LOGTAB_Q[LOGTAB_Q_TERMS - 1];
+  for (int k = LOGTAB_Q_TERMS - 2; k >= 0; k--) qp = fma_rn(qp, r, LOGTAB_Q[k]);
   const double r2 = mul(r, r);
   const double ed = (double)e;
-  const double hi = fma_rn(ed, ATANH2_LN2_HI, lhi);  // exact
-  double lo = fma_rn(ed, ATANH2_LN2_LO, llo);
+  const double hi = fma_rn(ed, LOGTAB_LN2_HI, lhi);  // exact
+  double lo = fma_rn(ed, LOGTAB_LN2_LO, llo);
   lo = add(lo, delta);
   lo = fma_rn(r2, qp, lo);
   // hi + r by Fast2Sum: hi is 0 (then S = r) or at least -ln c_1 > |r|

@@ -26,8 +26,8 @@
 //   sigma^2 - ln M  (crates/com-mapping/src/demapper.rs:82-146, :270-297), or with the
 //   exact demapper the log-sum-exp of each half of the labels.
 // f64 frames compute all of it in f64 with the correctly-rounded log/sin/cos of
-// crmath.cuh: bit-identical to the reference's draws up to the platform libm's last
-// bit.  f32 frames draw the same bits and the same uniforms, take the Gaussian in f32
+// crmath_fast.cuh (crmath.cuh's values): bit-identical to the reference's draws up to
+// the platform libm's last bit.  f32 frames draw the same bits and the same uniforms, take the Gaussian in f32
 // and the max-log LLRs per I/Q dimension (the Gray square QAM labels split into an
 // imaginary-part and a real-part Gray code, so the max-log LLRs separate exactly).
 #include <cuda_runtime.h>

@@ -1,5 +1,7 @@
 """Generate ``crmath_consts.inc``: double-double constants of the correctly-rounded
-f64 logarithm and sine/cosine used by the f64 noise kernels.
+f64 logarithm and sine/cosine used by the f64 noise kernels, and the tables of the fast
+sine/cosine (crmath_fast.cuh): sin and cos of j pi/128, j = 0..32, as double-doubles, and
+pi/128 as H1 + H2 + H3 with H1 a multiple of 2^-45 (j H1 exact for |j| <= 32).
 
 Constants are computed exactly (fractions) or to 60 decimal digits (decimal module):
 ln 2, pi/2 as three doubles, 1/(2k+1) for the atanh series of the logarithm and 1/n!
@@ -71,6 +73,44 @@ def main():
             a, b = split(Fraction((-1) ** k, fact))
             print(f"  {{{h(a)}, {h(b)}}},")
         print("};")
+    main_fast(pi)
+
+
+def sin_cos(x):
+    """sin and cos of the Decimal x by their Taylor series, to the context precision."""
+    s, c, term, k = Decimal(0), Decimal(0), Decimal(1), 0
+    while True:
+        if k % 4 == 0:
+            c += term
+        elif k % 4 == 1:
+            s += term
+        elif k % 4 == 2:
+            c -= term
+        else:
+            s -= term
+        k += 1
+        term = term * x / k
+        if abs(term) < Decimal(10) ** -75:
+            return s, c
+
+
+def main_fast(pi):
+    hh = pi / 128
+    h1 = Fraction(round(Fraction(str(hh)) * 2 ** 45), 2 ** 45)
+    assert float(h1) == h1
+    h2, h3 = split(Fraction(str(hh)) - h1)
+    print(f"#define CR_SC_H1 {h(float(h1))}")
+    print(f"#define CR_SC_H2 {h(h2)}")
+    print(f"#define CR_SC_H3 {h(h3)}")
+    print(f"#define CR_SC_INV_H {h(float(128 / pi))}")
+    print("#define CR_SC_N 33")
+    print("CR_CONST double CR_SC_TAB[CR_SC_N][4] = {  /* sin hi, sin lo, cos hi, cos lo of j pi/128 */")
+    for j in range(33):
+        sv, cv = sin_cos(hh * j)
+        a, b = split(sv)
+        c, d = split(cv)
+        print(f"  {{{h(a)}, {h(b)}, {h(c)}, {h(d)}}},")
+    print("};")
 
 
 if __name__ == "__main__":

@@ -1,4 +1,5 @@
-"""Generate ``atanh2_table.inc``: the table of the f64 2 atanh of the sum-product rule.
+"""Generate ``logtab.inc``: the logarithm table of the f64 2 atanh of the sum-product rule
+(atanh2.cuh) and of the fast correctly rounded log (crmath_fast.cuh).
 
 The logarithm follows Tang's table-driven method (P. T. P. Tang, "Table-driven
 implementation of the logarithm function in IEEE floating-point arithmetic", ACM TOMS
@@ -8,13 +9,13 @@ multiple of 2^-61, fits 53 bits: one fused multiply-add computes it exactly.  Fi
 log x = e ln 2 - ln c_j + log1p(r).
 
 Written here, each computed exactly (fractions) or to 60 digits (decimal module):
-  * ATANH2_LN2_HI: ln 2 rounded to a multiple of 2^-43, so that e * LN2_HI + L_hi is exact
-    for 0 <= e < 64; ATANH2_LN2_LO = RN(ln 2 - LN2_HI);
-  * ATANH2_TAB[j] = {c_j, L_hi_j, L_lo_j}, j = 0..256: L_hi_j = -ln c_j rounded to a multiple
+  * LOGTAB_LN2_HI: ln 2 rounded to a multiple of 2^-43, so that e * LN2_HI + L_hi is exact
+    for 0 <= e < 64; LOGTAB_LN2_LO = RN(ln 2 - LN2_HI);
+  * LOGTAB[j] = {c_j, L_hi_j, L_lo_j}, j = 0..256: L_hi_j = -ln c_j rounded to a multiple
     of 2^-43, L_lo_j = RN(-ln c_j - L_hi_j);
-  * ATANH2_Q: the Taylor coefficients (-1)^(k+1) / (k + 2), k = 0..5, of
+  * LOGTAB_Q: the Taylor coefficients (-1)^(k+1) / (k + 2), k = 0..5, of
     (log1p(r) - r) / r^2.
-Usage: ``python gen_atanh2_table.py > atanh2_table.inc``
+Usage: ``python gen_logtab.py > logtab.inc``
 """
 
 from decimal import Decimal, getcontext
@@ -51,12 +52,14 @@ def main():
     ln2 = Decimal(2).ln()
     ln2_hi = to_grid(ln2, -43)
     ln2_lo = float(Fraction(str(ln2)) - ln2_hi)
-    print("/* Table of the f64 2 atanh (Tang's table-driven logarithm).")
-    print("   Generated by gen_atanh2_table.py (exact fractions / 60-digit decimals). */")
-    print(f"#define ATANH2_LN2_HI {float(ln2_hi).hex()}")
-    print(f"#define ATANH2_LN2_LO {ln2_lo.hex()}")
-    print(f"#define ATANH2_TAB_N {N_TAB + 1}")
-    print("ATANH2_CONST double ATANH2_TAB[ATANH2_TAB_N][3] = {")
+    print("/* Tang's table-driven logarithm: the table of atanh2.cuh and crmath_fast.cuh.")
+    print("   Generated by gen_logtab.py (exact fractions / 60-digit decimals). */")
+    print("#pragma once")
+    print("#if defined(__CUDA_ARCH__)\n#define LOGTAB_CONST __device__ static const\n#else\n#define LOGTAB_CONST static const\n#endif")
+    print(f"#define LOGTAB_LN2_HI {float(ln2_hi).hex()}")
+    print(f"#define LOGTAB_LN2_LO {ln2_lo.hex()}")
+    print(f"#define LOGTAB_N {N_TAB + 1}")
+    print("LOGTAB_CONST double LOGTAB[LOGTAB_N][3] = {")
     for j in range(N_TAB + 1):
         c = c_of(j)
         L = -ln(c)
@@ -65,8 +68,8 @@ def main():
         assert float(c) == c and float(hi) == hi
         print(f"  {{{float(c).hex()}, {float(hi).hex()}, {lo.hex()}}},")
     print("};")
-    print(f"#define ATANH2_Q_TERMS {Q_TERMS}")
-    print("ATANH2_CONST double ATANH2_Q[ATANH2_Q_TERMS] = {")
+    print(f"#define LOGTAB_Q_TERMS {Q_TERMS}")
+    print("LOGTAB_CONST double LOGTAB_Q[LOGTAB_Q_TERMS] = {")
     for k in range(Q_TERMS):
         print(f"  {float(Fraction((-1) ** (k + 1), k + 2)).hex()},")
     print("};")

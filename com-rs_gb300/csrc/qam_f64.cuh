@@ -3,21 +3,22 @@
 #pragma once
 #include <cuda_runtime.h>
 
-#include "crmath.cuh"
+#include "crmath_fast.cuh"
 #include "device_common.cuh"
 
 namespace cbk {
 
 // Rng::complex_gaussian (crates/com-core/src/rng.rs:161-167): two uniforms u1, u2;
 // r = sqrt(-2 ln(1 - u1)) / sqrt(2); (r cos 2 pi u2, r sin 2 pi u2), with the correctly
-// rounded log, sin and cos of crmath.cuh
+// rounded log, sin and cos (the fast paths of crmath_fast.cuh, the same bits as
+// crmath.cuh's)
 __device__ __forceinline__ void complex_gaussian_f64(cbd::Xoshiro& r, double& nre, double& nim) {
   const double u1 = (double)(cbd::xoshiro_next(r) >> 11) * (1.0 / 9007199254740992.0);
   const double u2 = (double)(cbd::xoshiro_next(r) >> 11) * (1.0 / 9007199254740992.0);
-  const double l = crm::cr_log(__dsub_rn(1.0, u1));
+  const double l = crm::cr_log_fast(__dsub_rn(1.0, u1));
   const double rad = __dmul_rn(__dsqrt_rn(__dmul_rn(-2.0, l)), 0.70710678118654752440);
   double sn, cs;
-  crm::cr_sincos(__dmul_rn(6.283185307179586, u2), &sn, &cs);
+  crm::cr_sincos_fast(__dmul_rn(6.283185307179586, u2), &sn, &cs);
   nre = __dmul_rn(rad, cs);
   nim = __dmul_rn(rad, sn);
 }

@@ -71,11 +71,37 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, int pos, 
                                           T alpha) {
   const int d = c.row_start[row + 1] - c.row_start[row];
   const EdgeSlots es = c.tvars ? EdgeSlots{c.tvars, pos, c.m} : EdgeSlots{c.vars, c.row_start[row], 1};
-  if (RULE == cbd::RULE_SUM_PRODUCT) {
-    // the product of the other tanh(L/2) by prefix and suffix products.  The first pass
-    // keeps each edge's tanh(l/2) in the edge's message slot, whose old message it no
-    // longer needs, so that the second pass does not compute it again; layered, l goes to
-    // the variable's posterior (no other row of the level touches that variable).
+  if (RULE == cbd::RULE_SUM_PRODUCT && sizeof(T) == 4) {
+    // the product of the other tanh(L/2) by prefix and suffix products.  In f32 tanh is
+    // cheap: the second pass computes it again from the unchanged post and msg, which
+    // costs less than storing it (the messages of large codes live in global memory)
+    T prefix = (T)1;
+    for (int k = 0; k < d; k++) {
+      const int e = es.slot(k), v = es.var(k);
+      const T t = tanh_t(mul_rn(sub_rn(post[v], msg[e]), (T)0.5));
+      aux[e] = prefix;
+      prefix = mul_rn(prefix, t);
+    }
+    T suffix = (T)1;
+    for (int k = d - 1; k >= 0; k--) {
+      const int e = es.slot(k), v = es.var(k);
+      const T l = sub_rn(post[v], msg[e]);
+      const T t = tanh_t(mul_rn(l, (T)0.5));
+      const T p = mul_rn(aux[e], suffix);
+      suffix = mul_rn(suffix, t);
+      const T o = twice_atanh_t(p);
+      if (LAYERED) {
+        msg[e] = o;
+        post[v] = add_rn(l, o);
+      } else {
+        out[e] = o;
+      }
+    }
+  } else if (RULE == cbd::RULE_SUM_PRODUCT) {
+    // f64: the first pass keeps each edge's tanh(l/2) (34 FP64 instructions) in the edge's
+    // message slot, whose old message it no longer needs, so that the second pass does
+    // not compute it again; layered, l goes to the variable's posterior (no other row of
+    // the level touches that variable)
     T prefix = (T)1;
     for (int k = 0; k < d; k++) {
       const int e = es.slot(k), v = es.var(k);

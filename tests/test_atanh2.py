@@ -16,9 +16,9 @@ CSRC = os.path.join(HERE, "..", "com-rs_gb300", "csrc")
 
 
 def test_table_is_its_generator_output():
-    out = subprocess.run([sys.executable, os.path.join(CSRC, "gen_atanh2_table.py")], capture_output=True,
+    out = subprocess.run([sys.executable, os.path.join(CSRC, "gen_logtab.py")], capture_output=True,
                          text=True, check=True).stdout
-    assert out == open(os.path.join(CSRC, "atanh2_table.inc")).read()
+    assert out == open(os.path.join(CSRC, "logtab.inc")).read()
 
 
 @pytest.fixture(scope="module")
