@@ -633,8 +633,8 @@ LEARNED_POINTS = {"c5": {"learned": 6.97, "plain_20": 6.51, "plain_T": 7.33},
                   "c4": {"learned": 2.17, "plain_20": 2.09, "plain_T": 2.35}}
 LEARNED_FRAMES = {"c5": 8192, "c4": 65536}
 # dram__bytes_read.sum + dram__bytes_write.sum of one decode of a step's frames
-# (profiles/learned_decode_c5.md: 554,730,752 + 16,534,016 B)
-LEARNED_TRAFFIC = {"c5": 554_730_752 + 16_534_016}
+# (profiles/learned_decode_c5.md: 554,730,752 + 16,534,016 B; C4: 272,915,712 + 2,977,024 B)
+LEARNED_TRAFFIC = {"c5": 554_730_752 + 16_534_016, "c4": 272_915_712 + 2_977_024}
 LEARNED_METRIC = "decoded info Gbit/s at equal FER (1e-3), neural vs plain min-sum; vs CPU Runner"
 
 
