@@ -37,6 +37,13 @@ template <>
 __device__ __forceinline__ float infinity<float>() { return __int_as_float(0x7f800000); }
 
 // ---- syndrome test on packed hard decisions
+// post < 0 for the hard decision: in f64 the sign bit (an integer test), since the
+// posteriors are never -0.0 or NaN
+__device__ __forceinline__ uint32_t is_negative(double v) {
+  return (uint32_t)((unsigned long long)__double_as_longlong(v) >> 63);
+}
+__device__ __forceinline__ uint32_t is_negative(float v) { return (uint32_t)(v < 0.0f); }
+
 // hd holds, per base column j, the hard decisions of its Z bits packed 32 per word
 // (ceil(Z/32) words, then one zero word).  The parity of the 32 lifted rows
 // [32g, 32g + 32) of layer L is the XOR over the layer's entries (j, s) of the
@@ -48,7 +55,7 @@ __device__ __forceinline__ void build_hard_decisions(const T* post, uint32_t* hd
   for (int task = warp; task < ncol * wz; task += nw) {
     const int j = task / wz, w = task - j * wz;
     const int r = w * 32 + lane;
-    const uint32_t word = __ballot_sync(0xffffffffu, r < z && post[j * z + r] < (T)0);
+    const uint32_t word = __ballot_sync(0xffffffffu, r < z && is_negative(post[j * z + r]));
     if (lane == 0) {
       hd[j * ws + w] = word;
       if (w == wz - 1) hd[j * ws + wz] = 0u;
@@ -79,7 +86,7 @@ __device__ __forceinline__ bool some_check_fails(const T* post, uint32_t* hd, co
         const uint32_t en = ent[t];
         int cc = tid + (int)(en & 0xffffu);
         cc -= (cc >= z) ? z : 0;
-        par ^= (uint32_t)(post[(int)(en >> 16) * z + cc] < (T)0);
+        par ^= is_negative(post[(int)(en >> 16) * z + cc]);
       }
       bad = (int)par;
     }
@@ -123,9 +130,16 @@ __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t*
     unsigned c = (unsigned)r + (en & 0xffffu);
     unsigned cm = c - (unsigned)z;
     off[e] = (int)(en >> 16) * z + (int)min(c, cm);
-    T mag = (e == old_i1) ? a2 : a1;
-    T old = ((mt >> (8 + e)) & 1u) ? -mag : mag;
-    x[e] = sub_rn(post[off[e]], old);
+    if constexpr (sizeof(T) == 8) {
+      // the old message as bits: the magnitude (never negative) with the old sign ORed
+      // in, so that one subtraction is the FP64 work (p - (-m) is p + m, bit for bit)
+      const long long mb = __double_as_longlong(e == old_i1 ? a2 : a1);
+      x[e] = sub_rn(post[off[e]], __longlong_as_double(mb | ((long long)((mt >> (8 + e)) & 1u) << 63)));
+    } else {
+      T mag = (e == old_i1) ? a2 : a1;
+      T old = ((mt >> (8 + e)) & 1u) ? -mag : mag;
+      x[e] = sub_rn(post[off[e]], old);
+    }
   }
   // check_message, min-sum branch (ldpc.rs:468-491): sign product with `l < 0`, strict
   // `<` for the minimum and its index, min(m2, a) for the second (equal for non-NaN,
@@ -181,8 +195,8 @@ __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t*
     if constexpr (sizeof(T) == 8) {
       const long long bx = __double_as_longlong(x[e]);
       ng = par ^ (uint32_t)((unsigned long long)bx >> 63);
-      const T mag = (e == i1) ? n2 : n1;
-      o = __longlong_as_double(__double_as_longlong(mag) ^ ((long long)ng << 63));
+      const long long mb = e == i1 ? __double_as_longlong(n2) : __double_as_longlong(n1);
+      o = __longlong_as_double(mb ^ ((long long)ng << 63));
     } else {
       ng = par ^ (uint32_t)(x[e] < (T)0);
       T mag = (e == i1) ? n2 : n1;
