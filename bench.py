@@ -823,14 +823,14 @@ def run_spec_profile_case(args):
 
 def run_profile_case(args):
     """The small case the committed ncu summaries capture: `frames` C2 codewords generated
-    once (Eb/N0 = 1 dB), then decoded three times."""
+    once (Eb/N0 = 1 dB), then decoded three times, in --precision."""
     import torch
 
     cb = importlib.import_module("com-rs_gb300")
     L = cb.lib()
     n = args.frames
-    code = cb.NrLdpc(K_INFO, E, base_graph=BG, lifting_size=Z, precision="f32")
-    llr = torch.empty((n, E), dtype=torch.float32, device="cuda")
+    code = cb.NrLdpc(K_INFO, E, base_graph=BG, lifting_size=Z, precision=args.precision)
+    llr = torch.empty((n, E), dtype=torch.float32 if args.precision == "f32" else torch.float64, device="cuda")
     info = torch.empty((n, (K_INFO + 31) // 32), dtype=torch.int32, device="cuda")
     bits = torch.empty((n, (K_INFO + 31) // 32), dtype=torch.int32, device="cuda")
     iters = torch.empty(n, dtype=torch.int32, device="cuda")
@@ -898,6 +898,7 @@ def main():
                          "min-sum at equal FER; spec: the link of specs/bicm_ldpc.yaml")
     ap.add_argument("--protocol", choices=["c5", "c4"], default="c5", help="the code of --workload learned")
     ap.add_argument("--trials", type=int, default=2048, help="trials per step of --workload spec")
+    ap.add_argument("--precision", choices=["f32", "f64"], default="f32", help="the decoder of the c2 profile case")
     ap.add_argument("--profile-case", action="store_true",
                     help="generate --frames C2 codewords (--workload spec: --trials trials; mix: the batch; "
                          "learned: one step's frames) and decode them three times (for ncu)")
