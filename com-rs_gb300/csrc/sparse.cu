@@ -126,6 +126,45 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, int pos, 
         out[e] = o;
       }
     }
+  } else if (sizeof(T) == 8) {
+    // f64 min-sum with the reference's comparisons on the integer pipes: `l < 0` is the
+    // sign bit of a nonzero, non-NaN l (-0.0 and NaN compare false, as in f64), the
+    // magnitudes order as their bit patterns (NaN above infinity, so never `<`), and
+    // s * mag with s = +-1 is mag with its sign bit flipped.  The scaled magnitudes are
+    // the same for every edge, so they are computed once.  The results are the same
+    // bits as the branch below.
+    const long long kAbs = 0x7fffffffffffffffll, kInf = 0x7ff0000000000000ll;
+    int neg = 0, i1 = 0;
+    long long b1 = kInf, b2 = kInf;
+    for (int i = 0; i < d; i++) {
+      const long long bl = __double_as_longlong((double)sub_rn(post[es.var(i)], msg[es.slot(i)]));
+      const long long a = bl & kAbs;
+      neg ^= (int)(bl < 0 && a != 0 && a <= kInf);
+      if (a < b1) {
+        b2 = b1;
+        b1 = a;
+        i1 = i;
+      } else if (a < b2) {
+        b2 = a;
+      }
+    }
+    const T m1 = (T)__longlong_as_double(b1), m2 = (T)__longlong_as_double(b2);
+    const T n1 = RULE == cbd::RULE_NMS ? mul_rn(alpha, m1) : fmax(sub_rn(m1, alpha), (T)0);
+    const T n2 = RULE == cbd::RULE_NMS ? mul_rn(alpha, m2) : fmax(sub_rn(m2, alpha), (T)0);
+    for (int i = 0; i < d; i++) {
+      const int e = es.slot(i), v = es.var(i);
+      const T l = sub_rn(post[v], msg[e]);
+      const long long bl = __double_as_longlong((double)l), a = bl & kAbs;
+      const int sneg = neg ^ (int)(bl < 0 && a != 0 && a <= kInf);
+      const long long mb = __double_as_longlong((double)(i == i1 ? n2 : n1));
+      const T o = (T)__longlong_as_double(mb ^ ((long long)sneg << 63));
+      if (LAYERED) {
+        msg[e] = o;
+        post[v] = add_rn(l, o);
+      } else {
+        out[e] = o;
+      }
+    }
   } else {
     int neg = 0, i1 = 0;
     T m1 = infinity<T>(), m2 = infinity<T>();
