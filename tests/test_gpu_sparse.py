@@ -148,6 +148,27 @@ def test_nr_rows_through_the_generic_decoder_equal_the_nr_decoder(cb, O):
         assert np.array_equal(post[:, :520].view(np.uint64), app.view(np.uint64))
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("layered", [True, False])
+def test_min_sum_signed_zeros_and_extremes_equal_the_oracle(cb, O, layered, precision):
+    # channel LLRs of +0.0 and -0.0 (`l < 0` is false for both, though -0.0 has the sign
+    # bit) and of huge magnitudes, finite in the precision: posteriors and iterations
+    # equal the oracle's bit for bit
+    ref, gpu = _codes(cb, O, "peg_n576_k288.alist", "normalized_min_sum", 0.75, layered, 20, precision)
+    _, llr = _frames(O, ref, 1.5, 0, 64)
+    llr = llr.copy()
+    u = np.random.default_rng(3).random(llr.shape)
+    llr[u < 0.05] = 0.0
+    llr[(u >= 0.05) & (u < 0.10)] = -0.0
+    big = (u >= 0.10) & (u < 0.12)
+    llr[big] *= 1e250 if precision == "f64" else 1e30
+    dt = np.uint64 if precision == "f64" else np.uint32
+    post_g, it_g = gpu.decode_llr(llr)
+    post_o, it_o = ref.decode_llr_many(llr, precision)
+    assert np.array_equal(it_g, it_o)
+    assert np.array_equal(post_g.view(dt), post_o.view(dt))
+
+
 def test_edge_cases(cb):
     from test_sparse_host import HAMMING
 
