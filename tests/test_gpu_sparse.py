@@ -329,6 +329,30 @@ def test_set_decoder_equals_a_fresh_code(cb, O):
         assert np.array_equal(its, its_f), rule
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("rule, alpha", [("normalized_min_sum", 0.75), ("offset_min_sum", 0.3)])
+def test_dense_rows_take_the_warp_path_and_equal_the_oracle(cb, O, rule, alpha, precision):
+    # dense random rows (20 to 60 of 120 variables): levels of at most 8 rows, so one warp
+    # decodes each row with shuffle reductions of the minimum, its first index, the second
+    # minimum and the sign parity; signed zeros among the LLRs; min-sum bit for bit
+    rng = np.random.default_rng(11)
+    n, m = 120, 40
+    rows = [sorted(rng.choice(n, size=int(rng.integers(20, 61)), replace=False).tolist()) for _ in range(m)]
+    gpu = cb.Ldpc(n, rows, rule=rule, alpha=alpha, max_iterations=12, precision=precision, encoder=None)
+    assert gpu.info()["max_level_rows"] <= 8 and gpu.info()["max_row_degree"] <= 128
+    ref = O.Code(rows=rows, n=n)
+    ref.set_decoder({"normalized_min_sum": O.RULE_NMS, "offset_min_sum": O.RULE_OMS}[rule], alpha, True, 12)
+    llr = rng.normal(4.0, 2.0, (128, n))  # about half the frames stop early
+    llr[:, :4] = 0.0
+    llr[:40, 4:8] = -0.0
+    dt = np.uint64 if precision == "f64" else np.uint32
+    post_g, it_g = gpu.decode_llr(llr)
+    post_o, it_o = ref.decode_llr_many(llr, precision)
+    assert np.array_equal(it_g, it_o)
+    assert np.array_equal(post_g.view(dt), post_o.view(dt))
+    assert (it_g < 12).any() and (it_g == 12).any()
+
+
 @pytest.mark.parametrize("n, m, dmax, seed", [(300, 150, 6, 1), (1200, 900, 5, 2), (2000, 600, 14, 3),
                                               (4000, 2000, 8, 4)])
 def test_random_codes_equal_the_oracle(cb, O, n, m, dmax, seed):
