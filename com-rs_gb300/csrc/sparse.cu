@@ -293,6 +293,49 @@ __device__ __forceinline__ void check_row_warp(const SparseDev& c, int row, T* p
         post[c.vars[e]] = add_rn(l_r[k], o);
       }
     }
+  } else if (sizeof(T) == 8) {
+    // f64: the integer forms of check_row's f64 min-sum (the same bits); the reduction
+    // keeps the first index among equal minima, as the strict `<` of the sequential loop
+    const long long kAbs = 0x7fffffffffffffffll, kInf = 0x7ff0000000000000ll;
+    int neg = 0, i1 = 0x7fffffff;
+    long long b1 = kInf, b2 = kInf;
+    for (int e = e0 + lane; e < e1; e += 32) {
+      const long long bl = __double_as_longlong((double)sub_rn(post[c.vars[e]], msg[e]));
+      const long long a = bl & kAbs;
+      neg ^= (int)(bl < 0 && a != 0 && a <= kInf);
+      if (a < b1) {
+        b2 = b1;
+        b1 = a;
+        i1 = e - e0;
+      } else if (a < b2) {
+        b2 = a;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long bb1 = __shfl_xor_sync(0xffffffffu, b1, o);
+      const long long bb2 = __shfl_xor_sync(0xffffffffu, b2, o);
+      const int bi1 = __shfl_xor_sync(0xffffffffu, i1, o);
+      neg ^= __shfl_xor_sync(0xffffffffu, neg, o);
+      const bool mine = b1 < bb1 || (b1 == bb1 && i1 < bi1);
+      const long long w2 = mine ? b2 : bb2, l1 = mine ? bb1 : b1;
+      b1 = mine ? b1 : bb1;
+      i1 = mine ? i1 : bi1;
+      b2 = w2 < l1 ? w2 : l1;
+    }
+    const T m1 = (T)__longlong_as_double(b1), m2 = (T)__longlong_as_double(b2);
+    const T n1 = RULE == cbd::RULE_NMS ? mul_rn(alpha, m1) : fmax(sub_rn(m1, alpha), (T)0);
+    const T n2 = RULE == cbd::RULE_NMS ? mul_rn(alpha, m2) : fmax(sub_rn(m2, alpha), (T)0);
+    for (int e = e0 + lane; e < e1; e += 32) {
+      const int v = c.vars[e];
+      const T l = sub_rn(post[v], msg[e]);
+      const long long bl = __double_as_longlong((double)l), a = bl & kAbs;
+      const int sneg = neg ^ (int)(bl < 0 && a != 0 && a <= kInf);
+      const long long mb = __double_as_longlong((double)((e - e0) == i1 ? n2 : n1));
+      const T o = (T)__longlong_as_double(mb ^ ((long long)sneg << 63));
+      msg[e] = o;
+      post[v] = add_rn(l, o);
+    }
   } else {
     int neg = 0, i1 = 0x7fffffff;
     T m1 = infinity<T>(), m2 = infinity<T>();
@@ -349,7 +392,7 @@ __device__ __forceinline__ bool some_row_fails(const SparseDev& c, const T* post
 // REGS: the layered sum-product rows keep their tanh values and prefix products in
 // registers (check_row_spa_regs; every row of at most kRegRowDegree edges)
 template <typename T, int RULE, bool LAYERED, bool REGS>
-__global__ void __launch_bounds__(512) sparse_kernel(const __grid_constant__ SparseArgs<T> a) {
+__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1) sparse_kernel(const __grid_constant__ SparseArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SparseDev& c = a.code;
   const int tid = threadIdx.x, nt = blockDim.x;
