@@ -320,6 +320,9 @@ SPEC_WORKLOAD = ("specs/bicm_ldpc.yaml link: PEG(1024, 512) var degree 3 seed 1,
 # algorithmic bytes of one decoded codeword through cb_ldpc_decode_device: n f64 LLRs in,
 # n f64 posteriors out, a 4-byte iteration count
 SPEC_ALGO_BYTES = SPEC_N * 8 * 2 + 4
+# dram__bytes_read.sum + dram__bytes_write.sum of one f64 decode of 2048 trials at 2.5 dB
+# (profiles/spec_link_sparse.md: 141,528,576 + 90,683,392 B)
+SPEC_TRAFFIC = 141_528_576 + 90_683_392
 
 
 def spec_cpu_sample(steps, warmup, threads=0, budget_s=2.0):
@@ -452,7 +455,9 @@ def run_spec_ours(args, rank, world, local_rank):
     peaks = read_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "sparse_group_kernel<double, sum-product, register rows> (generic decoder, several codewords "
+                "traffic": SPEC_TRAFFIC, "traffic_source": "ncu capture of one f64 decode of 2048 trials at 2.5 dB "
+                                                          "(bench.py --workload spec --profile-case --trials 2048)",
+                "kernel": "sparse_group_kernel<double, sum-product, register rows> (generic decoder, several codewords "
                           "per CTA)",
                 "algorithmic_bytes_per_launch": T * SPEC_BLOCKS * SPEC_ALGO_BYTES, "launch_ms": dec,
                 "mean_iterations": float(iters.float().mean()),
