@@ -42,7 +42,7 @@ FRAME_DTYPE = np.dtype([("bit_errors", "<u4"), ("frame_error", "u1"), ("iteratio
 class ComrsError(RuntimeError):
     """A non-zero status of the C ABI (``cb_status``), with the library's message."""
 
-    KINDS = {-1: "Config", -2: "Shape", -3: "Numerical", -4: "Condition", -5: "Io", -6: "Cuda", -7: "Timeout"}
+    KINDS = {-1: "Config", -2: "Shape", -3: "Numerical", -4: "Condition", -5: "Io", -6: "Cuda"}
 
     def __init__(self, status, message):
         self.status = status

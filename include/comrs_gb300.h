@@ -35,9 +35,11 @@ typedef enum {
   CB_ERR_NUMERICAL = -3, /* Error::Numerical */
   CB_ERR_CONDITION = -4, /* Error::Condition */
   CB_ERR_IO = -5,        /* Error::Io */
-  CB_ERR_CUDA = -6,      /* a CUDA call failed */
-  CB_ERR_TIMEOUT = -7    /* a bounded device wait ran out */
+  CB_ERR_CUDA = -6       /* a CUDA call failed */
 } cb_status;
+/* No kernel of this library waits on another kernel, another CTA or the host: work is
+ * handed out by atomic counters and every launch ends on its own, so no call has a
+ * device wait that could time out. */
 
 typedef enum { CB_RULE_SUM_PRODUCT = 0, CB_RULE_NMS = 1, CB_RULE_OMS = 2 } cb_rule;
 typedef enum { CB_F64 = 0, CB_F32 = 1 } cb_precision;

@@ -111,3 +111,48 @@ def test_two_process_campaign_equals_one_process(cb, O):
                  seed=7, name=NAME, batch=50)
     want = [(r.trials, r.record["fer"].errors, r.record["ber"].errors, r.record["iterations"].total) for r in one]
     assert out[0] == out[1] == want
+
+
+def test_statistics_known_answers_of_the_reference(cb):
+    # crates/com-sim/src/stats.rs:20-36 (module example), :230-249
+    # (wilson_with_no_error_and_merges); crates/com-math/src/special.rs:221-224, :286-289
+    c = cb.campaign
+    e = c.ErrorRate()
+    e.add(3, 1000)
+    e.add(7, 1000)
+    assert e.rate() == 5e-3
+    lo, hi = e.wilson(0.95)
+    assert lo < 5e-3 < hi
+    m = c.Mean()
+    for v in (1.0, 2.0, 3.0, 4.0):
+        m.add(v)
+    assert (m.mean(), m.variance()) == (2.5, 5.0 / 3.0)
+    assert abs(c.z_score(0.95) - 1.959964) < 1e-5
+    assert abs(c.qfuncinv(0.025) - 1.959964) < 1e-6
+    q = 0.5 * c.erfc(c.qfuncinv(1e-6) / 2 ** 0.5)
+    assert abs(q / 1e-6 - 1.0) < 1e-9
+    assert abs(c.erfc(1.0) / 0.15729920705028513 - 1.0) < 1e-15
+    assert abs(c.erfc(10.0) / 2.0884875837625448e-45 - 1.0) < 1e-15
+    lo, hi = c.ErrorRate(0, 1000).wilson(0.95)
+    assert lo == 0.0 and abs(hi - 3.83e-3) < 1e-4
+    import math
+
+    a, b, whole = c.Mean(), c.Mean(), c.Mean()
+    for i in range(100):
+        v = math.sin(i * 0.37)
+        (a if i < 30 else b).add(v)
+        whole.add(v)
+    a.merge(b)
+    assert abs(a.mean() - whole.mean()) < 1e-14 and abs(a.variance() - whole.variance()) < 1e-14
+
+
+def test_integer_batches_give_the_exact_mean_and_variance(cb):
+    import numpy as np
+
+    c = cb.campaign
+    x = np.random.default_rng(1).integers(0, 21, 5000)
+    m = c.Mean()
+    for part in np.array_split(x, 7):
+        m.add_counts(len(part), int(part.sum()), int((part * part).sum()))
+    assert m.count() == 5000 and m.total == int(x.sum())
+    assert abs(m.mean() - x.mean()) < 1e-12 and abs(m.variance() - x.var(ddof=1)) < 1e-9
