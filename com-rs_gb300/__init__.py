@@ -93,6 +93,7 @@ SYMBOLS = [
     ("cb_mix_set_rows_per_thread", _i32, [_vp, _i32, _i32]),
     ("cb_mix_run", _i32, [_vp, _u64, _vp]),
     ("cb_mix_time_decode", _i32, [_vp, _i32, _i32, C.POINTER(_dbl)]),
+    ("cb_mix_frames", _i32, [_vp, _u64, _vp, _vp]),
     ("cb_decode_device_noalloc", _i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
     ("cb_xoshiro_jump", _i32, [_vp, _u64, _vp]),
     ("cb_ldpc_create", _i32, [_i32, _i32, _vp, _vp, _i32, _dbl, _i32, _i32, _i32, _i32, C.POINTER(_vp)]),
@@ -203,6 +204,16 @@ class NrLdpc:
         self.precision = precision
         self.dtype = np.float64 if precision == "f64" else np.float32
         self.rule, self.alpha, self.max_iterations = rule_l, alpha, max_iterations
+
+    DECODERS = {-1: "not yet on a device", 0: "generic layered", 1: "base-graph layered min-sum",
+                2: "layered min-sum compiled for this lifting"}
+
+    @property
+    def decoder(self):
+        """The decoder kernel this code runs (cb_code_info field 15), once it has been on a device."""
+        info = np.zeros(16, np.int64)
+        _check(lib().cb_code_info(self._h, _p(info)), self._h)
+        return self.DECODERS[int(info[15])]
 
     def close(self):
         if getattr(self, "_h", None):

@@ -22,7 +22,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-f
               "--expt-relaxed-constexpr"] + ARCH
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
-CU = ["decode.cu", "gen.cu", "nms_learned.cu", "mix.cu", "sparse.cu", "sparse_encode.cu", "link.cu", "nr_generic.cu", "capi.cu",
+CU = ["decode.cu", "decode_nr.cu", "gen.cu", "nms_learned.cu", "mix.cu", "sparse.cu", "sparse_encode.cu", "link.cu", "nr_generic.cu", "capi.cu",
       "capi_mix.cu", "capi_sparse.cu"]
 CPP = ["code_host.cpp", "sparse_host.cpp"]
 
@@ -32,6 +32,33 @@ def _nvcc():
         if cand and os.path.exists(cand):
             return cand
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build comrs_gb300")
+
+
+# the kernel source files the library compiles again at run time (NVRTC), embedded as text
+JIT_FILES = ["dev_math.cuh", "nr_bg_schedule.inc", "layered_nr.cuh"]
+JIT_INC = "nr_jit_sources.inc"
+
+
+def _write_jit_sources(out_dir):
+    """`<out_dir>/nr_jit_sources.inc`: the files of JIT_FILES as C++ raw string literals
+    (rewritten only when their text changes, so that the object depending on it stays
+    fresh otherwise)."""
+    parts = ["// Generated by build.py: the decoder's kernel sources for the run-time compiler.\n",
+             f"static const int kJitFileCount = {len(JIT_FILES)};\n",
+             "static const char* const kJitFileNames[] = {" + ", ".join(f'"{f}"' for f in JIT_FILES) + "};\n",
+             "static const char* const kJitFileTexts[] = {\n"]
+    for f in JIT_FILES:
+        text = open(os.path.join(CSRC, f)).read()
+        if ")cbjit" in text:
+            raise RuntimeError(f"{f} contains the raw-string delimiter")
+        parts.append('R"cbjit(' + text + ')cbjit",\n')
+    parts.append("};\n")
+    body = "".join(parts)
+    path = os.path.join(out_dir, JIT_INC)
+    if not os.path.exists(path) or open(path).read() != body:
+        with open(path, "w") as fh:
+            fh.write(body)
+    return path
 
 
 def _stale(obj, deps):
@@ -46,11 +73,12 @@ def build(verbose=False, extra_flags=(), out_dir=None, lib=None):
     nvcc = _nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     headers.append(os.path.join(HERE, "..", "include", "comrs_gb300.h"))
+    headers.append(_write_jit_sources(OUT))
     jobs = []
     for f in CU:
         src, obj = os.path.join(CSRC, f), os.path.join(OUT, f + ".o")
         if _stale(obj, [src] + headers):
-            jobs.append([nvcc, *NVCC_FLAGS, *extra_flags, "-c", src, "-o", obj])
+            jobs.append([nvcc, *NVCC_FLAGS, *extra_flags, "-I", OUT, "-c", src, "-o", obj])
     for f in CPP:
         src, obj = os.path.join(CSRC, f), os.path.join(OUT, f + ".o")
         if _stale(obj, [src] + headers):
@@ -68,7 +96,7 @@ def build(verbose=False, extra_flags=(), out_dir=None, lib=None):
         list(ex.map(run, jobs))
     objs = [os.path.join(OUT, f + ".o") for f in CU + CPP]
     if jobs or not os.path.exists(LIBP):
-        run([nvcc, *ARCH, "-shared", "-o", LIBP, *objs, "-lcudart"])
+        run([nvcc, *ARCH, "-shared", "-o", LIBP, *objs, "-lcudart", "-ldl"])
     return LIBP
 
 

@@ -14,6 +14,7 @@
 #include "code_host.h"
 #include "dev_code.h"
 #include "kernels.h"
+#include "nr_decode.h"
 
 #define CB_VERSION_STRING "comrs_gb300 0.1.0 (sm_103a)"
 
@@ -74,6 +75,13 @@ struct cb_code {
   size_t post_cap = 0;
   int32_t* d_giters = nullptr;
   size_t giters_cap = 0;
+  // f32 layered min-sum: the graph-specialised decoder (layered_nr.cuh), its launch
+  // parameters (the code part filled once) and why it is not the code's own build, if not
+  bool use_nr = false;
+  cbk::NrKernel nr;
+  cbn::NrArgs nr_args;
+  std::string nr_note;
+  int noalloc_grid = 0;  // resident CTAs of cb_decode_device_noalloc's kernel (0: not yet known)
 };
 
 namespace {
@@ -145,6 +153,23 @@ template <typename T>
 cb_status decode_device_impl(cb_code* c, const T* llr, int64_t n, uint32_t* bits, T* app, int32_t* iters,
                              const uint32_t* ref, cbd::FrameResult* results, cudaStream_t s) {
   if (c->generic) return generic_decode_impl<T>(c, llr, n, bits, app, iters, ref, results, s);
+  if constexpr (sizeof(T) == 4) {
+    if (c->use_nr) {
+      cbn::NrArgs& a = c->nr_args;
+      a.llr = llr;
+      a.n_frames = n;
+      a.bits_out = bits;
+      a.app_out = app;
+      a.iters_out = iters;
+      a.ref_bits = ref;
+      a.results = reinterpret_cast<cbn::FrameRecord*>(results);
+      a.state = reinterpret_cast<unsigned char*>(c->d_state);
+      a.work_counter = c->d_counter;
+      CB_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), s));
+      CB_CUDA(c, cbk::nr_launch(c->nr, a, (int)std::min<int64_t>(c->decode_grid, n), s));
+      return CB_OK;
+    }
+  }
   cbk::DecodeArgs<T> a;
   a.code = c->dev;
   a.cfg = c->cfg;
@@ -343,7 +368,32 @@ cb_status ensure_device(cb_code* c) {
   v.map = c->d_map;
   v.inv_start = c->d_inv_start;
   v.inv_t = c->d_inv_t;
-  c->decode_grid = cbk::decode_grid_size(v, c->precision, c->device);
+  // f32 layered min-sum: the graph-specialised decoder, built for this code's lifting when
+  // the run-time compiler is at hand, else the base graph's build
+  if (c->precision == CB_F32 && !c->generic && c->cfg.layered &&
+      (c->cfg.rule == cbd::RULE_NMS || c->cfg.rule == cbd::RULE_OMS)) {
+    c->nr = cbk::nr_kernel(h, c->device, true, &c->nr_note);
+    int g = c->nr.fn ? cbk::nr_grid_size(c->nr, h, c->device) : 0;
+    if (g <= 0 && c->nr.specialized) {
+      cudaGetLastError();
+      c->nr_note = "the specialised decoder's occupancy query failed";
+      c->nr = cbk::nr_kernel(h, c->device, false, nullptr);
+      g = cbk::nr_grid_size(c->nr, h, c->device);
+    }
+    if (g > 0) {
+      c->use_nr = true;
+      c->decode_grid = g;
+      cbk::fill_nr_args(h, c->nr_args);
+      c->nr_args.map = c->d_map;
+      c->nr_args.inv_start = c->d_inv_start;
+      c->nr_args.inv_t = c->d_inv_t;
+      c->nr_args.max_iterations = c->cfg.max_iterations;
+      c->nr_args.rule = c->cfg.rule;
+      c->nr_args.alpha = (float)c->cfg.alpha;
+    }
+    cudaGetLastError();
+  }
+  if (!c->use_nr) c->decode_grid = cbk::decode_grid_size(v, c->precision, c->device);
   if (c->decode_grid <= 0) return fail(c, CB_ERR_CUDA, "the decoder does not fit an SM (occupancy 0)");
   CB_CUDA(c, cudaMalloc(&c->d_state, cbk::decode_state_bytes_per_slot(v, c->precision) * c->decode_grid));
   c->dev_ready = true;
@@ -442,8 +492,10 @@ cb_status cb_code_set_demapper(cb_code* c, int32_t exact) {
 cb_status cb_code_info(const cb_code* c, int64_t info[16]) {
   if (!c || !info) return fail(nullptr, CB_ERR_CONFIG, "NULL argument");
   const cbh::NrCode& h = c->host;
+  const int64_t kind = !c->dev_ready ? -1 : !c->use_nr ? 0 : c->nr.specialized ? 2 : 1;
   int64_t v[16] = {h.bg, h.z, h.k_info, h.e, h.k, h.n_full, (int64_t)h.rows_n * h.z, h.edges, h.ils, h.max_degree,
-                   h.rv, h.qm, (int64_t)h.core_terms.size(), h.map_is_offset ? 1 : 0, (int64_t)h.entry_col.size(), 0};
+                   h.rv, h.qm, (int64_t)h.core_terms.size(), h.map_is_offset ? 1 : 0, (int64_t)h.entry_col.size(),
+                   kind};
   std::memcpy(info, v, sizeof v);
   return CB_OK;
 }
@@ -1001,14 +1053,42 @@ cb_status noalloc_scratch(cb_code* c, int device, void** out) {
 template <typename T>
 cb_status decode_noalloc_impl(cb_code* c, void* scratch, const T* llr, int64_t n, uint32_t* bits, int32_t* iters,
                               cudaStream_t s) {
-  const size_t slot = cbk::decode_state_bytes_per_slot(c->dev, c->precision);
+  // f32 layered min-sum runs the base graph's graph-specialised decoder (built into this
+  // library: a run-time compiled module would allocate device memory when it loads)
+  const bool nr = sizeof(T) == 4 && (c->cfg.rule == cbd::RULE_NMS || c->cfg.rule == cbd::RULE_OMS);
+  const cbk::NrKernel k = nr ? cbk::nr_kernel(c->host, c->device, false, nullptr) : cbk::NrKernel{};
+  const bool use_nr = nr && k.fn;
+  const size_t slot = use_nr ? cbn::nr_state_bytes(c->host.rows_n * c->host.z)
+                             : cbk::decode_state_bytes_per_slot(c->dev, c->precision);
   const int64_t fit = (int64_t)((kNoallocScratchBytes - kNoallocCounterBytes) / slot);
   if (fit < 1)
     return fail(c, CB_ERR_SHAPE,
                 "the check-node state of one CTA (" + std::to_string(slot) + " bytes) exceeds the " +
                     std::to_string(kNoallocScratchBytes >> 20) + " MiB scratch of cb_decode_device_noalloc");
-  const int occupancy = cbk::decode_grid_size(c->dev, c->precision, c->device);
+  if (c->noalloc_grid <= 0)  // the occupancy query once per code object
+    c->noalloc_grid = use_nr ? cbk::nr_grid_size(k, c->host, c->device)
+                             : cbk::decode_grid_size(c->dev, c->precision, c->device);
+  const int occupancy = c->noalloc_grid;
   if (occupancy <= 0) return fail(c, CB_ERR_CUDA, "the decoder does not fit an SM (occupancy 0)");
+  // the work counter must start at zero; the state slots need no clearing (the first
+  // iteration of every codeword reads no state)
+  CB_CUDA(c, cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), s));
+  const int grid = (int)std::min<int64_t>(std::min<int64_t>(occupancy, fit), n);
+  if (use_nr) {
+    cbn::NrArgs a;
+    cbk::fill_nr_args(c->host, a);
+    a.max_iterations = c->cfg.max_iterations;
+    a.rule = c->cfg.rule;
+    a.alpha = (float)c->cfg.alpha;
+    a.llr = reinterpret_cast<const float*>(llr);
+    a.n_frames = n;
+    a.bits_out = bits;
+    a.iters_out = iters;
+    a.work_counter = reinterpret_cast<unsigned long long*>(scratch);
+    a.state = reinterpret_cast<unsigned char*>(scratch) + kNoallocCounterBytes;
+    CB_CUDA(c, cbk::nr_launch(k, a, grid, s));
+    return CB_OK;
+  }
   cbk::DecodeArgs<T> a;
   a.code = c->dev;
   a.cfg = c->cfg;
@@ -1023,10 +1103,6 @@ cb_status decode_noalloc_impl(cb_code* c, void* scratch, const T* llr, int64_t n
   a.work_counter = reinterpret_cast<int32_t*>(scratch);
   a.state = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(scratch) + kNoallocCounterBytes);
   a.status = nullptr;
-  // the work counter must start at zero; the state slots need no clearing (the first
-  // iteration of every codeword reads no state)
-  CB_CUDA(c, cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), s));
-  const int grid = (int)std::min<int64_t>(std::min<int64_t>(occupancy, fit), n);
   CB_CUDA(c, cbk::launch_decode<T>(a, grid, s));
   return CB_OK;
 }

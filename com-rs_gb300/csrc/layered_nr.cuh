@@ -1,0 +1,353 @@
+// Layered normalised/offset min-sum decoding of 5G NR LDPC codewords in f32, with the base
+// graph's structure fixed at compile time.
+//
+// Restates LdpcCode::propagate and check_message (crates/com-fec/src/ldpc.rs:449-557) on
+// the lifted NR graphs of crates/com-fec/src/nr/ldpc.rs:124-134, with the LLR placement of
+// NrLdpc::full_llr (nr/ldpc.rs:191-197): the algorithm, the state layout and the results
+// of the generic layered decoder (decode.cu), bit for bit.
+//
+// What is fixed at compile time: the rows of the base graph, their degrees and columns,
+// and the level schedule (rows of one level share no column and run between the same two
+// barriers).  Each row's update is specialised to its degree and to its entries'
+// positions in the launch parameters, and the whole iteration is one straight-line body.
+// The lifting is a policy: `RuntimeLifting` reads Z and the shifts from the launch
+// parameters (the library's nvcc build, any code of the base graph); a `FixedLifting`
+// with Z and all shifts as constants is generated per code and compiled at run time by
+// NVRTC (decode_nr.cu), which turns every edge address into an immediate offset.
+//
+// This file is also NVRTC source: it includes only dev_math.cuh and the generated
+// schedule, and uses no host headers.
+#pragma once
+#include "dev_math.cuh"
+
+namespace cbn {
+using namespace cbk;
+
+#include "nr_bg_schedule.inc"
+
+template <int BG>
+struct Graph;
+template <>
+struct Graph<1> : BaseGraph1 {};
+template <>
+struct Graph<2> : BaseGraph2 {};
+
+constexpr int kMaxEntries = 316;
+constexpr int kMaxRows = 46;
+
+// the per-frame record (cbd::FrameResult, cb_frame_result)
+struct FrameRecord {
+  uint32_t bit_errors;
+  uint8_t frame_error;
+  uint8_t iterations;
+  uint16_t reserved;
+};
+
+// Launch parameters (plain data, the same layout under nvcc and NVRTC).
+struct NrArgs {
+  int32_t z, n_full, k, k_info, e, rows, n_entries;
+  int32_t map_kind;          // 0: output bit t is full-word bit 2Z + t; 1: `map`; 2: `inv_*` (repeats)
+  const int32_t* map;        // [E] full-word position of output bit t
+  const int32_t* inv_start;  // [n_full + 1]
+  const int32_t* inv_t;      // [E] output bits of full-word bit v, in increasing order
+  int32_t max_iterations;
+  int32_t rule;              // 1: normalised min-sum, 2: offset min-sum
+  float alpha;               // the scale or the offset
+  int32_t reserved;
+  const float* llr;          // [n_frames][E]
+  int64_t n_frames;
+  uint32_t* bits_out;        // [n_frames][ceil(K'/32)] (optional)
+  float* app_out;            // [n_frames][K'] (optional)
+  int32_t* iters_out;        // [n_frames] (optional)
+  const uint32_t* ref_bits;  // [n_frames][ceil(K'/32)] sent bits (optional)
+  FrameRecord* results;      // [n_frames] (optional)
+  unsigned char* state;      // per resident CTA: nr_state_bytes(rows Z)
+  unsigned long long* work_counter;  // zeroed before the launch
+  uint32_t entry[kMaxEntries];       // (column << 16) | shift, row-major
+  uint2 eaddr[kMaxEntries];          // {4 shift, 4 column Z}
+  uint16_t layer_start[kMaxRows + 1];
+};
+
+// the check-node state of a CTA: an 8-byte plane {n1, n2} and a 4-byte plane of meta words
+// (bits 0-4 an edge holding the second minimum, bits 8.. the outgoing signs)
+__host__ __device__ inline size_t nr_state_bytes(int lifted_rows) {
+  return (((size_t)lifted_rows * 12) + 255) & ~(size_t)255;
+}
+
+__host__ __device__ inline size_t nr_smem_bytes(int n_full, int z, int rows, int n_entries) {
+  const int ws = (z + 31) / 32 + 1;
+  size_t b = (size_t)n_full * 4;
+  b += (size_t)(n_full / z) * ws * 4;  // packed hard decisions
+  b += (size_t)n_entries * 4;           // entries
+  b += (size_t)(rows + 1) * 2 + 16;     // layer starts
+  return (b + 15) & ~(size_t)15;
+}
+
+// Z and the shifts from the launch parameters
+struct RuntimeLifting {
+  static constexpr bool fixed = false;
+  static constexpr int z = 0;
+  static constexpr int shift[1] = {0};
+};
+
+// Byte offset in the posteriors of entry T's variable for lifted row r (r4 = 4 r):
+// 4 (column Z + (r + shift) mod Z).
+template <int BG, class K, int T>
+__device__ __forceinline__ int edge_offset(const NrArgs& a, int r, int r4, int z4) {
+  if constexpr (K::fixed) {
+    constexpr int sh = K::shift[T], c = Graph<BG>::col[T];
+    return r >= K::z - sh ? r4 + 4 * (c * K::z + sh - K::z) : r4 + 4 * (c * K::z + sh);
+  } else {
+    // r + shift < 2Z: (r + shift) mod Z is the unsigned minimum of u and u - Z
+    const uint2 t = a.eaddr[T];
+    const uint32_t u = (uint32_t)r4 + t.x;
+    return (int)(t.y + __viaddmin_u32(u, (uint32_t)-z4, u));
+  }
+}
+
+// the edge offsets of a row, entries S0 + I .. S0 + D - 1 (a compile-time loop)
+template <int BG, class K, int S0, int I, int D>
+__device__ __forceinline__ void row_offsets(int (&off)[D], const NrArgs& a, int r, int r4, int z4) {
+  if constexpr (I < D) {
+    off[I] = edge_offset<BG, K, S0 + I>(a, r, r4, z4);
+    row_offsets<BG, K, S0, I + 1, D>(off, a, r, r4, z4);
+  }
+}
+
+__device__ __forceinline__ float ld_f(const unsigned char* post, int off) {
+  return *reinterpret_cast<const float*>(post + off);
+}
+__device__ __forceinline__ void st_f(unsigned char* post, int off, float v) {
+  *reinterpret_cast<float*>(post + off) = v;
+}
+
+// One lifted row of base row L (degree D, entries S0 ..): old state (a1, a2, mt) -> new
+// state (n1, n2, nm), posteriors updated in place.  The operations of row_update_lean
+// (decode_common.cuh), with the addresses from edge_offset.
+template <int BG, class K, int S0, int D>
+__device__ __forceinline__ void nr_row(unsigned char* post, const NrArgs& a, int r, int r4, int z4, float a1,
+                                       float a2, uint32_t mt, bool nms, float alpha, float& n1, float& n2,
+                                       uint32_t& nm) {
+  int off[D];
+  float x[D];
+  const int old_i1 = (int)(mt & 31u);
+  const uint32_t t0 = mt << (24 - D);  // the old sign of edge 0 at bit 31
+  row_offsets<BG, K, S0, 0, D>(off, a, r, r4, z4);
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    const float mag = (i == old_i1) ? a2 : a1;
+    // p - (s ? -mag : mag) as p + (the negated old message)
+    const uint32_t neg = (__float_as_uint(mag) ^ 0x80000000u) ^ ((t0 << i) & 0x80000000u);
+    x[i] = __fadd_rn(ld_f(post, off[i]), __uint_as_float(neg));
+  }
+  float m1 = __int_as_float(0x7f800000), m2 = __int_as_float(0x7f800000);
+#pragma unroll
+  for (int i = 0; i + 1 < D; i += 2) {
+    const float s = min_xorsign_abs(x[i], x[i + 1]);
+    const float l = fmaxf(fabsf(x[i]), fabsf(x[i + 1]));
+    m2 = min3f(m2, fmaxf(fabsf(m1), fabsf(s)), l);
+    m1 = min_xorsign_abs(m1, s);
+  }
+  if (D & 1) {
+    m2 = fminf(m2, fmaxf(fabsf(m1), fabsf(x[D - 1])));
+    m1 = min_xorsign_abs(m1, x[D - 1]);
+  }
+  const uint32_t ps = __float_as_uint(m1) & 0x80000000u;
+  m1 = fabsf(m1);
+  if (nms) {
+    n1 = __fmul_rn(alpha, m1);
+    n2 = __fmul_rn(alpha, m2);
+  } else {
+    n1 = fmaxf(__fsub_rn(m1, alpha), 0.0f);
+    n2 = fmaxf(__fsub_rn(m2, alpha), 0.0f);
+  }
+  const uint32_t n1p = __float_as_uint(n1) | ps, n2p = __float_as_uint(n2) | ps;
+  uint32_t sm = 0;
+  int i1 = 0;
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    const bool eq = fabsf(x[i]) == m1;
+    const uint32_t magp = eq ? n2p : n1p;
+    i1 = eq ? i : i1;
+    const uint32_t ob = magp ^ (__float_as_uint(x[i]) & 0x80000000u);
+    st_f(post, off[i], __fadd_rn(x[i], __uint_as_float(ob)));
+    sm = (sm << 1) | (ob >> 31);
+  }
+  nm = (sm << 8) | (uint32_t)i1;
+}
+
+struct NrState {
+  unsigned char* mag;
+  unsigned char* meta;
+  uint64_t pol;
+  __device__ __forceinline__ void load(int row, float& a1, float& a2, uint32_t& mt) const {
+    uint32_t x, y, w;
+    asm volatile("ld.global.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+                 : "=r"(x), "=r"(y)
+                 : "l"(mag + (size_t)row * 8), "l"(pol));
+    asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(w) : "l"(meta + (size_t)row * 4), "l"(pol));
+    a1 = __uint_as_float(x);
+    a2 = __uint_as_float(y);
+    mt = w;
+  }
+  __device__ __forceinline__ void store(int row, float n1, float n2, uint32_t nm) const {
+    asm volatile("st.global.L2::cache_hint.v2.u32 [%0], {%1, %2}, %3;" ::"l"(mag + (size_t)row * 8),
+                 "r"(__float_as_uint(n1)), "r"(__float_as_uint(n2)), "l"(pol)
+                 : "memory");
+    asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(meta + (size_t)row * 4), "r"(nm), "l"(pol)
+                 : "memory");
+  }
+};
+
+// One layered iteration: the rows in schedule order, a barrier after each level.
+template <int BG, class K, int Q>
+__device__ __forceinline__ void nr_iteration(unsigned char* post, const NrArgs& a, const NrState& st, int r, int r4,
+                                             int z4, int z, bool active, bool first, bool nms, float alpha) {
+  if constexpr (Q < Graph<BG>::rows) {
+    constexpr int L = Graph<BG>::order[Q];
+    constexpr int S0 = Graph<BG>::start[L];
+    constexpr int D = Graph<BG>::start[L + 1] - S0;
+    if (active) {
+      // the row index passes through an empty asm so that the compiler recomputes each
+      // row's addresses where they are used instead of hoisting all of them out of the
+      // iteration loop (they would not fit in registers)
+      int rr = r, rr4 = r4;
+      asm volatile("" : "+r"(rr), "+r"(rr4));
+      const int zz = K::fixed ? K::z : z;
+      float a1 = 0.0f, a2 = 0.0f, n1, n2;
+      uint32_t mt = 0, nm;
+      if (!first) st.load(L * zz + rr, a1, a2, mt);
+      nr_row<BG, K, S0, D>(post, a, rr, rr4, z4, a1, a2, mt, nms, alpha, n1, n2, nm);
+      st.store(L * zz + rr, n1, n2, nm);
+    }
+    if constexpr (Graph<BG>::level_end[Q] != 0) __syncthreads();
+    nr_iteration<BG, K, Q + 1>(post, a, st, r, r4, z4, z, active, first, nms, alpha);
+  }
+}
+
+// Persistent kernel: each CTA takes codewords from the work counter, one thread per
+// lifted row, posteriors in shared memory, check-node state in its own L2-resident slot.
+template <int BG, class K>
+__global__ void __launch_bounds__(384, 2) layered_nr_kernel(const __grid_constant__ NrArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int z = K::fixed ? K::z : a.z;
+  const int nt = blockDim.x, tid = threadIdx.x;
+  const int n_full = a.n_full, ncol = n_full / z;
+  const int ws = (z + 31) / 32 + 1;
+  float* post = reinterpret_cast<float*>(smem);
+  uint32_t* hd = reinterpret_cast<uint32_t*>(post + n_full);
+  uint32_t* s_ent = hd + ncol * ws;
+  uint16_t* s_lstart = reinterpret_cast<uint16_t*>(s_ent + a.n_entries);
+  __shared__ long long s_cw;
+  __shared__ unsigned int s_err;
+  const int lifted = a.rows * z;
+  unsigned char* slot = a.state + (size_t)blockIdx.x * nr_state_bytes(lifted);
+  const NrState st{slot, slot + (size_t)lifted * 8, l2_evict_last_policy()};
+  const bool nms = a.rule == 1;
+  const float alpha = a.alpha;
+  const int max_it = a.max_iterations;
+  const int wpf = (a.k_info + 31) >> 5;
+  const bool active = tid < z;
+  const int r4 = 4 * tid, z4 = 4 * z;
+  for (int i = tid; i < a.n_entries; i += nt) s_ent[i] = a.entry[i];
+  for (int i = tid; i <= a.rows; i += nt) s_lstart[i] = a.layer_start[i];
+
+  for (;;) {
+    if (tid == 0) {
+      s_cw = (long long)atomicAdd(a.work_counter, 1ull);
+      s_err = 0;
+    }
+    __syncthreads();
+    const long long cw = s_cw;
+    if (cw >= a.n_frames) break;
+
+    // ---- channel LLRs of the full word (NrLdpc::full_llr): 0.0 + LLR, punctured and
+    // unsent bits 0.0, fillers KNOWN_BIT_LLR
+    const float* llr = a.llr + (size_t)cw * a.e;
+    for (int v = tid; v < n_full; v += nt) post[v] = 0.0f;
+    __syncthreads();
+    if (a.map_kind == 0) {
+      if ((a.e & 3) == 0 && (reinterpret_cast<uintptr_t>(a.llr) & 15) == 0) {
+        const float4* l4 = reinterpret_cast<const float4*>(llr);
+        for (int q = tid; q < (a.e >> 2); q += nt) {
+          const float4 v = __ldcs(l4 + q);
+          float* d = post + 2 * z + 4 * q;
+          d[0] = __fadd_rn(0.0f, v.x);
+          d[1] = __fadd_rn(0.0f, v.y);
+          d[2] = __fadd_rn(0.0f, v.z);
+          d[3] = __fadd_rn(0.0f, v.w);
+        }
+      } else {
+        for (int t = tid; t < a.e; t += nt) post[2 * z + t] = __fadd_rn(0.0f, __ldcs(llr + t));
+      }
+    } else if (a.map_kind == 1) {
+      for (int t = tid; t < a.e; t += nt) post[a.map[t]] = __fadd_rn(0.0f, __ldcs(llr + t));
+    } else {
+      for (int v = tid; v < n_full; v += nt) {
+        const int b0 = a.inv_start[v], b1 = a.inv_start[v + 1];
+        if (b0 == b1) continue;
+        float s = 0.0f;
+        for (int i = b0; i < b1; i++) s = __fadd_rn(s, llr[a.inv_t[i]]);
+        post[v] = s;
+      }
+    }
+    __syncthreads();
+    for (int v = a.k_info + tid; v < a.k; v += nt) post[v] = 30.0f;  // KNOWN_BIT_LLR, signal.rs:37
+    __syncthreads();
+
+    // ---- propagate (ldpc.rs:509-551): syndrome test before the first iteration and after each
+    int it = 0;
+    if (some_check_fails(post, hd, s_ent, s_lstart, a.rows, ncol, z, tid, nt)) {
+      it = max_it;
+      for (int iter = 1; iter <= max_it; iter++) {
+        nr_iteration<BG, K, 0>(reinterpret_cast<unsigned char*>(post), a, st, tid, r4, z4, z, active, iter == 1, nms,
+                               alpha);
+        if (!some_check_fails(post, hd, s_ent, s_lstart, a.rows, ncol, z, tid, nt)) {
+          it = iter;
+          break;
+        }
+      }
+    }
+
+    // ---- outputs: hard decisions (signal.rs:47-49), counts (errors.rs:39-42); the decision
+    // words are staged in hd and written 16 bytes at a time when the row of words allows it
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    unsigned int be = 0;
+    for (int b0 = warp * 32; b0 < a.k_info; b0 += nw * 32) {
+      const int v = b0 + lane;
+      const bool bit = v < a.k_info && post[v] < 0.0f;
+      const uint32_t word = __ballot_sync(0xffffffffu, bit);
+      if (lane == 0) {
+        hd[b0 >> 5] = word;
+        if (a.ref_bits) be += __popc(word ^ a.ref_bits[(size_t)cw * wpf + (b0 >> 5)]);
+      }
+    }
+    __syncthreads();
+    if (a.bits_out) {
+      uint32_t* dst = a.bits_out + (size_t)cw * wpf;
+      if ((wpf & 3) == 0 && (reinterpret_cast<uintptr_t>(a.bits_out) & 15) == 0) {
+        for (int q = tid; q < (wpf >> 2); q += nt) reinterpret_cast<uint4*>(dst)[q] = reinterpret_cast<const uint4*>(hd)[q];
+      } else {
+        for (int w = tid; w < wpf; w += nt) dst[w] = hd[w];
+      }
+    }
+    if (a.app_out)
+      for (int v = tid; v < a.k_info; v += nt) a.app_out[(size_t)cw * a.k_info + v] = post[v];
+    if (be) atomicAdd(&s_err, be);
+    __syncthreads();
+    if (tid == 0) {
+      if (a.iters_out) a.iters_out[cw] = it;
+      if (a.results) {
+        FrameRecord rec;
+        rec.bit_errors = s_err;
+        rec.frame_error = s_err > 0;
+        rec.iterations = (uint8_t)it;
+        rec.reserved = 0;
+        a.results[cw] = rec;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace cbn

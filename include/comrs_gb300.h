@@ -90,7 +90,11 @@ cb_status cb_code_set_demapper(cb_code* code, int32_t exact);
 
 /* info[0..16): base graph, Z, K', E, K (systematic columns), n_full, lifted rows,
  * edges, iLS, max row degree, rv, qm, core-inverse terms, 1 if the rate matching is
- * the plain offset 2Z + t, 0, 0. */
+ * the plain offset 2Z + t, base-graph entries, and the decoder that runs: -1 before the
+ * code's first device call, 0 the generic layered decoder (f64, sum-product, flooding),
+ * 1 the f32 layered min-sum built for the base graph, 2 the same compiled at run time for
+ * this code's lifting size (Z and every shift as constants; needs libnvrtc, see
+ * COMRS_NO_JIT and COMRS_JIT_CACHE in the integration notes). */
 cb_status cb_code_info(const cb_code* code, int64_t info[16]);
 
 /* The construction tables: `entries` = n_entries records (base row, base column,
@@ -221,6 +225,11 @@ cb_status cb_mix_set_rows_per_thread(cb_mix* mix, int32_t class_index, int32_t r
 cb_status cb_mix_run(cb_mix* mix, uint64_t epoch, cb_frame_result* out);
 /* the best of `reps` event-timed decode phases of one class (-1: all classes) */
 cb_status cb_mix_time_decode(cb_mix* mix, int32_t class_index, int32_t reps, double* ms);
+/* The frames the batch's generator writes at `epoch` (one replay): the f32 channel LLRs
+ * the decoder reads and the K' information bits, in the items' order (item i's E_i LLRs,
+ * then item i + 1's; llr: sum of E_i floats, info: sum of K'_i bytes 0/1; either may be
+ * NULL).  For checks of the decoder against a reference decoder on the same LLRs. */
+cb_status cb_mix_frames(cb_mix* mix, uint64_t epoch, float* llr, uint8_t* info);
 
 /* ---- Generic sparse LDPC codes: LdpcCode::decode_llr (crates/com-fec/src/ldpc.rs:497-505)
  * for any parity-check matrix given by its rows (LdpcCode::from_rows / from_alist,

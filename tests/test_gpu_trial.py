@@ -2,7 +2,9 @@
 
 f64: the E channel LLRs and the K' info bits of every frame are bit-identical to the
 oracle's (correctly-rounded noise mode), and so are the per-frame bit errors, frame
-errors and iteration counts.  f32: same bits, noise in f32, statistically equal FER.
+errors and iteration counts.  f32: same bits, noise in f32, statistically equal FER;
+on the timed configuration (BG1 Z = 384, 16-QAM) the f32 trial is compared with the
+oracle's f64 trial with the platform libm's noise at the waterfall and on the bench grid.
 """
 
 import numpy as np
@@ -102,6 +104,67 @@ def test_frames_do_not_depend_on_the_batching(cb, O):
                             g.run_frames(7, NAME, 1, 1334, 1766, 1.0, 4)])
     assert np.array_equal(whole, parts)
     assert np.array_equal(whole, g.run_frames(7, NAME, 1, 100, 3000, 1.0, 4))
+
+
+def _overlap(a, b, confidence=0.99):
+    (a0, a1), (b0, b1) = a.wilson(confidence), b.wilson(confidence)
+    return not (a1 < b0 or b1 < a0)
+
+
+def _paired_z(x, y):
+    d = np.asarray(x, np.float64) - np.asarray(y, np.float64)
+    sd = d.std(ddof=1)
+    return 0.0 if sd == 0 else d.mean() / (sd / np.sqrt(len(d)))
+
+
+def _ber_agrees(x, y, bits_per_frame, z=3.3):
+    # The bit errors of a frame come in bursts (a failed frame has hundreds), so the bits
+    # are not independent trials and a binomial interval over bits is far too narrow; the
+    # frames are independent, so the BER's standard error is that of the mean per-frame
+    # count.  The two BERs agree when they differ by less than z of those errors.
+    x, y = np.asarray(x, np.float64), np.asarray(y, np.float64)
+    se = np.hypot(x.std(ddof=1) / np.sqrt(len(x)), y.std(ddof=1) / np.sqrt(len(y)))
+    return abs(x.mean() - y.mean()) <= z * se, (x.mean() / bits_per_frame, y.mean() / bits_per_frame)
+
+
+# The timed configuration (benchmark config 2: BG1 Z = 384, 16-QAM, f32 generator and f32
+# decoder through cb_run_frames) against the oracle's f64 trial with the platform libm's
+# noise, i.e. the reference's own arithmetic (crates/com-core/src/rng.rs:161-167,
+# crates/com-channel/src/awgn.rs:139-141, crates/com-fec/src/ldpc.rs:509-557).  Both draw
+# every frame from the same stream, so besides the 99 % Wilson overlap of the rates
+# (validation/tests/aff3ct.rs:265-338) and of the bit error rates (frame-clustered), the
+# frames can be compared in pairs: most end alike, and the per-frame differences of bit
+# errors and iterations centre on zero.
+@pytest.mark.parametrize("eb,n,cond", [(2.6, 1024, 31), (2.7, 3072, 32)])
+def test_c2_f32_trial_matches_the_oracle_at_the_waterfall(cb, O, eb, n, cond):
+    from conftest import load_package
+
+    ErrorRate = load_package().campaign.ErrorRate
+    g32, r = codes(cb, O, CODES[4], "f32")
+    a = g32.run_frames(7, NAME, cond, 0, n, eb, 16)
+    b = r.run_frames(16, 7, O.fnv1a64(NAME), cond, 0, n, eb, 0, O.NOISE_LIBM, 0)
+    fa, fb = int(a["frame_error"].sum()), int(b["frame_error"].sum())
+    assert fb >= 200, fb  # enough frame errors for the comparison to mean something
+    assert _overlap(ErrorRate(fa, n), ErrorRate(fb, n)), (fa, fb)
+    ok, bers = _ber_agrees(a["bit_errors"], b["bit_errors"], 8448)
+    assert ok, bers
+    assert np.mean(a["frame_error"] == b["frame_error"]) >= 0.85
+    assert abs(_paired_z(a["bit_errors"], b["bit_errors"])) < 3.3
+    assert abs(_paired_z(a["iterations"], b["iterations"])) < 3.3
+
+
+def test_c2_f32_trial_ber_on_the_bench_grid(cb, O):
+    # 2 dB, the top of the benchmark grid: every frame fails (FER 1), so the bit errors
+    # are the informative count
+    n, eb = 256, 2.0
+    g32, r = codes(cb, O, CODES[4], "f32")
+    a = g32.run_frames(7, NAME, 30, 0, n, eb, 16)
+    b = r.run_frames(16, 7, O.fnv1a64(NAME), 30, 0, n, eb, 0, O.NOISE_LIBM, 0)
+    assert a["frame_error"].all() and b["frame_error"].all()
+    assert (a["iterations"] == 20).all() and (b["iterations"] == 20).all()
+    ok, bers = _ber_agrees(a["bit_errors"], b["bit_errors"], 8448)
+    assert ok, bers
+    assert abs(_paired_z(a["bit_errors"], b["bit_errors"])) < 3.3
 
 
 def test_large_code_high_snr_decodes_everything(cb, O):

@@ -61,3 +61,48 @@ def test_no_alloc_rejects_codes_it_cannot_serve(cb):
     with pytest.raises(cb.ComrsError) as ei:
         cb._check(cb.lib().cb_decode_device_noalloc(code._h, C.c_void_p(1), 1, None, None, None), code._h)
     assert ei.value.kind == "Config" and "plain rate matching" in str(ei.value)
+
+
+def test_no_alloc_first_call_on_a_fresh_code_allocates_nothing(cb):
+    # A code object whose first device call is cb_decode_device_noalloc: free device memory
+    # (cudaMemGetInfo) is the same before and after two calls, the object does no device
+    # set-up of its own, and the decisions equal the allocating decoder's.  A warm-up call
+    # on another object first loads the library's kernels (the first launch of a module
+    # maps its code into device memory; that is not an allocation by the entry point).
+    import torch
+
+    case = CASES[1]
+    kw = dict(base_graph=case["bg"], lifting_size=case["z"], precision=case["precision"])
+    warm = cb.NrLdpc(case["k"], case["e"], **kw)
+    llr_host, _ = warm.generate_frames(7, "no_alloc_fresh", 0, 0, 64, case["ebn0"], case["m"])
+    llr = torch.from_numpy(llr_host).to(device="cuda", dtype=torch.float32)
+    n, words = 64, (case["k"] + 31) // 32
+    L = cb.lib()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    bits = torch.full((n, words), -1, dtype=torch.int32, device="cuda")
+    iters = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    want_bits = torch.full((n, words), -1, dtype=torch.int32, device="cuda")
+    want_iters = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    args = (C.c_void_p(llr.data_ptr()), n, C.c_void_p(bits.data_ptr()), C.c_void_p(iters.data_ptr()), stream)
+    assert L.cb_decode_device_noalloc(warm._h, *args) == 0
+    assert L.cb_decode_device(warm._h, C.c_void_p(llr.data_ptr()), n, C.c_void_p(want_bits.data_ptr()), None,
+                              C.c_void_p(want_iters.data_ptr()), stream) == 0
+    torch.cuda.synchronize()
+    want = (want_bits.cpu().numpy(), want_iters.cpu().numpy())
+    bits.fill_(-1)
+    iters.fill_(-1)
+    torch.cuda.synchronize()
+    fresh = cb.NrLdpc(case["k"], case["e"], **kw)
+    for _ in range(2):
+        free_before = torch.cuda.mem_get_info()[0]
+        st = L.cb_decode_device_noalloc(fresh._h, *args)
+        torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
+        assert st == 0, L.cb_last_error(fresh._h).decode()
+        assert free_after == free_before
+        got = (bits.cpu().numpy(), iters.cpu().numpy())
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+        bits.fill_(-1)
+        iters.fill_(-1)
+        torch.cuda.synchronize()
+    assert fresh.decoder == "not yet on a device"
