@@ -67,7 +67,34 @@ ALGO_BYTES = E * 4 + (K_INFO + 7) // 8 + 4
 DRAM_BYTES_PER_CODEWORD = (208_447_232 + 71_422_976) / 2048
 WARP_INST_PER_CODEWORD_ITERATION = 4_894_572_480 / (2048 * 20)
 WORKLOAD = ("5G NR LDPC BG1 Z=384 K'=8448 E=25344 (rate 1/3), Gray 16-QAM, AWGN Eb/N0 0:0.25:2 dB, "
-            "max-log LLRs, layered NMS alpha=0.75, <=20 iterations + syndrome stop, f32, 8192 codewords/launch")
+            "max-log LLRs, layered NMS alpha=0.75, <=20 iterations + syndrome stop, 8192 codewords/launch")
+# a point at the code's waterfall (FER about 0.13; the grid above sits at FER 1)
+WATERFALL_DB = 2.7
+
+
+def c2_config(world, frames):
+    """The workload description both arms print (the arithmetic type is the line's dtype)."""
+    return {"workload": WORKLOAD, "codewords_per_launch": frames, "ebn0_db": GRID,
+            "l2": "inputs larger than L2: each step writes and reads 830 MB of LLRs",
+            "parallelism": f"dp{world} (disjoint frame ranges per GPU)"}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return None
 
 
 def read_peaks():
@@ -177,13 +204,14 @@ def run_reference(args, rank):
     if rank != 0:
         return
     gbps, cores, n, frames, t, fer = cpu_sample(args.steps, args.warmup)
-    sample = (f"{n} frames per step ({frames} in {args.steps} steps, {t:.1f} s) of the same workload, "
-              f"one frame per Runner trial, f64 decoder and libm noise as the reference")
+    sample = (f"{n} frames per step ({frames} in {args.steps} steps, {t:.1f} s, FER {fer:.3f}) of the same "
+              f"workload, one frame per Runner trial, f64 decoder and libm noise as the reference")
     line = {"impl": "reference", "metric": METRIC, "value": gbps, "unit": "Gbit/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "frames_per_step": n, "fer": fer},
-            "cpu_baseline": {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port", "sample": sample},
+            "config": c2_config(args.gpus, args.frames),
+            "cpu_baseline": {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port", "sample": sample,
+                             "cpu_model": cpu_model()},
             "e2e": {"value": gbps, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -289,22 +317,71 @@ def run_ours(args, rank, world, local_rank):
            "d2h_bytes_per_step": B * 8, "api": "cb_run_frames (host records)",
            "inputs": "the frames' streams (seed, name, condition, frame index) passed as arguments"}
 
+    # the BlockCode drop-in end to end (NrLdpc::decode_block, nr/ldpc.rs:216-220): one step's
+    # f32 LLRs in pinned host memory -> cb_decode -> packed decisions and iteration counts
+    # in host memory; the copies both ways are inside the timed call
+    llr_host = torch.empty((B, E), dtype=torch.float32, pin_memory=True)
+    llr_host.copy_(llr)
+    bits_host = torch.empty((B, (K_INFO + 7) // 8), dtype=torch.uint8, pin_memory=True)
+    it_host = torch.empty(B, dtype=torch.int32, pin_memory=True)
+    bc_args = (h, C.c_void_p(llr_host.data_ptr()), B, C.c_void_p(bits_host.data_ptr()), None,
+               C.c_void_p(it_host.data_ptr()))
+    st = L.cb_decode(*bc_args)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        st |= L.cb_decode(*bc_args)
+    barrier()
+    bc_s = max_over_ranks((time.perf_counter() - t0) / 3)
+    if st:
+        raise cb.ComrsError(st, L.cb_last_error(h).decode())
+    e2e_blockcode = {"value": B * world * K_INFO / bc_s / 1e9, "unit": "Gbit/s", "h2d_bytes_per_step": B * E * 4,
+                     "d2h_bytes_per_step": B * ((K_INFO + 7) // 8) + B * 4, "ms_per_step": bc_s * 1e3,
+                     "api": "cb_decode (pinned host f32 LLRs in; host packed decisions and iteration counts out)",
+                     "mean_iterations": float(it_host.float().mean())}
+
+    # the same trial at the code's waterfall, where the syndrome stop and the FER matter
+    wf = []
+    for s in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = L.cb_run_frames_device(h, M, SEED, nh, 9, (s * world + rank) * B, B, WATERFALL_DB,
+                                    C.c_void_p(results.data_ptr()), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if st:
+            raise cb.ComrsError(st, L.cb_last_error(h).decode())
+        r = results.cpu().numpy().view(cb.FRAME_DTYPE)
+        if s:
+            wf.append((max_over_ranks(e0.elapsed_time(e1)), r))
+    wf_ms = float(np.mean([x[0] for x in wf]))
+    wf_rec = np.concatenate([x[1] for x in wf])
+    waterfall = {"ebn0_db": WATERFALL_DB, "value": B * world * K_INFO / (wf_ms * 1e-3) / 1e9, "unit": "Gbit/s",
+                 "fer": float(wf_rec["frame_error"].mean()), "frame_errors": int(wf_rec["frame_error"].sum()),
+                 "frames": int(len(wf_rec)) * world, "mean_iterations": float(wf_rec["iterations"].mean()),
+                 "ms_per_step": wf_ms}
+
+    # neural vs plain min-sum at equal FER (the metric's comparison), on the learned
+    # decoder's own code (benchmark config 5) with the protocol's committed weights
+    decoders, _, _, _ = learned_decoders("c5", 2, 1, world, rank, local_rank, barrier, max_over_ranks)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         gbps, cores, n, frames, t, _ = cpu_sample(2, 0, budget_s=5.0)
+        gbps1, _, n1, frames1, t1, _ = cpu_sample(1, 0, threads=1, budget_s=4.0)
         cpu = {"value": gbps, "unit": "Gbit/s", "cores": cores, "kind": "port",
                "sample": f"{frames} frames ({t:.1f} s) of the same workload, grid points 0 and 0.25 dB, f64 decoder "
-                         f"and libm noise as the reference"}
+                         f"and libm noise as the reference; one thread: {frames1} frames ({t1:.1f} s) at 0 dB",
+               "value_1_thread": gbps1, "cpu_model": cpu_model()}
     if rank == 0:
+        config = c2_config(world, B)
+        config.update({"last_step_fer": fer_acc[-1], "last_step_mean_iterations": it_acc[-1],
+                       "waterfall": waterfall, "decoders": decoders})
         line = {"metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (Monte Carlo frames from seeded streams)",
-                "config": {"workload": WORKLOAD, "codewords_per_launch": B, "ebn0_db": GRID,
-                           "l2": "inputs larger than L2: each step writes and reads 830 MB of LLRs",
-                           "parallelism": f"dp{world} (disjoint frame ranges per GPU)",
-                           "last_step_fer": fer_acc[-1], "last_step_mean_iterations": it_acc[-1]},
-                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
-                "gpu_launches": 2 * args.steps}
+                "config": config, "e2e": e2e, "e2e_blockcode": e2e_blockcode, "roofline": roofline,
+                "cpu_baseline": cpu, "clocks": clocks.summary(), "gpu_launches": 2 * args.steps}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -694,13 +771,15 @@ def run_learned_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def run_learned_ours(args, rank, world, local_rank):
-    import torch
-
-    dist, barrier, max_over_ranks = start_ranks(world, local_rank)
-    cb, Lm, p = learned_setup(args.protocol)
-    B = LEARNED_FRAMES[args.protocol]
-    pts = LEARNED_POINTS[args.protocol]
+def learned_decoders(proto, steps, warmup, world, rank, local_rank, barrier, max_over_ranks, frames=None):
+    """Neural vs plain min-sum at equal FER: the learned decoder (the protocol's committed
+    weights) at its FER 1e-3 Eb/N0, the plain decoder at 20 iterations and at the learned
+    one's iteration count at theirs.  Each runs `steps` batches through its public call
+    (generation, decoding, records to the host), timed on the host clock.  Returns
+    ({decoder: figures}, the clocks of the learned decoder's run, its code, its network)."""
+    cb, Lm, p = learned_setup(proto)
+    B = frames or LEARNED_FRAMES[proto]
+    pts = LEARNED_POINTS[proto]
 
     def nr(it):
         return cb.NrLdpc(p["k"], p["e"], base_graph=p["bg"], lifting_size=p["z"], precision="f32",
@@ -708,29 +787,40 @@ def run_learned_ours(args, rank, world, local_rank):
 
     code = nr(p["T"])
     net = cb.LearnedNms(code, p["T"], shared=p["shared"])
-    Lm.load(net, os.path.join(ROOT, "com-rs_gb300", "weights", f"learned_{args.protocol}.npz"))
+    Lm.load(net, os.path.join(ROOT, "com-rs_gb300", "weights", f"learned_{proto}.npz"))
     decoders = {"learned": (net.run_frames, pts["learned"]), "plain_20": (nr(20).run_frames, pts["plain_20"]),
                 f"plain_{p['T']}": (nr(p["T"]).run_frames, pts["plain_T"])}
-
     out, clocks_summary = {}, None
     for key, (run, eb) in decoders.items():
-        for s in range(args.warmup):
+        for s in range(warmup):
             run(3, "learned_bench", 1, 10_000_000 + s * B, B, eb, p["m"])
         barrier()
         recs = []
         with ClockSampler(local_rank) as clocks:
             t0 = time.perf_counter()
-            for s in range(args.steps):
+            for s in range(steps):
                 recs.append(run(3, "learned_bench", 0, (s * world + rank) * B, B, eb, p["m"]))
             barrier()
             wall = max_over_ranks(time.perf_counter() - t0)
         r = np.concatenate(recs)
-        out[key] = {"value": args.steps * world * B * p["k"] / wall / 1e9, "unit": "Gbit/s", "ebn0_db": eb,
+        out[key] = {"value": steps * world * B * p["k"] / wall / 1e9, "unit": "Gbit/s", "ebn0_db": eb,
                     "fer": float(r["frame_error"].mean()), "frame_errors": int(r["frame_error"].sum()),
                     "frames": int(len(r)) * world, "mean_iterations": float(r["iterations"].mean()),
-                    "ms_per_step": wall / args.steps * 1e3}
+                    "ms_per_step": wall / steps * 1e3}
         if key == "learned":
             clocks_summary = clocks.summary()
+    return out, clocks_summary, code, net
+
+
+def run_learned_ours(args, rank, world, local_rank):
+    import torch
+
+    dist, barrier, max_over_ranks = start_ranks(world, local_rank)
+    cb, Lm, p = learned_setup(args.protocol)
+    B = LEARNED_FRAMES[args.protocol]
+    pts = LEARNED_POINTS[args.protocol]
+    out, clocks_summary, code, net = learned_decoders(args.protocol, args.steps, args.warmup, world, rank,
+                                                      local_rank, barrier, max_over_ranks)
     lv = out["learned"]
     # roofline of the learned decoder kernel: one step's frames generated into HBM, then
     # cb_nms_decode_device timed with CUDA events on torch's stream (the LLRs exceed L2)

@@ -400,6 +400,38 @@ cb_status cb_mix_run(cb_mix* m, uint64_t epoch, cb_frame_result* out) {
   return CB_OK;
 }
 
+cb_status cb_mix_frames(cb_mix* m, uint64_t epoch, float* llr, uint8_t* info) {
+  if (!m) return mfail(nullptr, CB_ERR_CONFIG, "NULL argument");
+  std::lock_guard<std::mutex> lock(m->mu);
+  MIX_CUDA(m, cudaSetDevice(m->device));
+  if (cb_status st = ensure_graph(m)) return st;
+  MIX_CUDA(m, cudaMemcpyAsync(m->d_epoch, &epoch, 8, cudaMemcpyHostToDevice, m->stream));
+  MIX_CUDA(m, cudaGraphLaunch(m->exec, m->stream));
+  std::vector<float> h_llr((size_t)m->llr_elems);
+  std::vector<uint32_t> h_info((size_t)m->info_words);
+  MIX_CUDA(m, cudaMemcpyAsync(h_llr.data(), m->d_llr, 4 * h_llr.size(), cudaMemcpyDeviceToHost, m->stream));
+  MIX_CUDA(m, cudaMemcpyAsync(h_info.data(), m->d_info, 4 * h_info.size(), cudaMemcpyDeviceToHost, m->stream));
+  MIX_CUDA(m, cudaStreamSynchronize(m->stream));
+  // the caller's layout: the items in their own order, each item's E LLRs and K' bits
+  std::vector<int64_t> lo((size_t)m->n + 1, 0), io((size_t)m->n + 1, 0);
+  std::vector<const cbk::MixItem*> by_index((size_t)m->n);
+  for (const cbk::MixItem& it : m->items) by_index[(size_t)it.index] = &it;
+  for (int64_t i = 0; i < m->n; i++) {
+    const cbh::NrCode& h = m->codes[by_index[(size_t)i]->code];
+    lo[(size_t)i + 1] = lo[(size_t)i] + h.e;
+    io[(size_t)i + 1] = io[(size_t)i] + h.k_info;
+  }
+  for (int64_t i = 0; i < m->n; i++) {
+    const cbk::MixItem& it = *by_index[(size_t)i];
+    const cbh::NrCode& h = m->codes[it.code];
+    if (llr) std::memcpy(llr + lo[(size_t)i], h_llr.data() + it.llr_offset, sizeof(float) * h.e);
+    if (info)
+      for (int b = 0; b < h.k_info; b++)
+        info[io[(size_t)i] + b] = (uint8_t)((h_info[(size_t)it.info_offset + (b >> 5)] >> (b & 31)) & 1u);
+  }
+  return CB_OK;
+}
+
 cb_status cb_mix_time_decode(cb_mix* m, int32_t cls, int32_t reps, double* ms) {
   if (!m || !ms || reps < 1 || cls < -1 || cls >= (int32_t)m->classes.size())
     return mfail(m, CB_ERR_CONFIG, "bad arguments");

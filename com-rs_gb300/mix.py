@@ -101,6 +101,16 @@ class MixBatch:
         self._check(self._lib.cb_mix_run(self._h, epoch, C.c_void_p(out.ctypes.data)))
         return out
 
+    def frames(self, epoch=0):
+        """The generator's frames at `epoch`: ([E_i f32 LLRs], [K'_i info bits]) per item, in
+        the items' order (the LLRs the decoder reads)."""
+        e = self.items["e"].astype(np.int64)
+        k = self.items["k_info"].astype(np.int64)
+        llr = np.zeros(int(e.sum()), np.float32)
+        info = np.zeros(int(k.sum()), np.uint8)
+        self._check(self._lib.cb_mix_frames(self._h, epoch, C.c_void_p(llr.ctypes.data), C.c_void_p(info.ctypes.data)))
+        return np.split(llr, np.cumsum(e)[:-1]), np.split(info, np.cumsum(k)[:-1])
+
     def time_decode(self, cls=-1, reps=3):
         ms = C.c_double()
         self._check(self._lib.cb_mix_time_decode(self._h, cls, reps, C.byref(ms)))

@@ -898,43 +898,54 @@ static inline size_t widx(const Learned& L, int t, int entry, int r) {
 
 static double softplus(double x) { return x > 0 ? x + std::log1p(std::exp(-x)) : std::log1p(std::exp(x)); }
 static double sigmoid(double x) { return x >= 0 ? 1.0 / (1.0 + std::exp(-x)) : std::exp(x) / (1.0 + std::exp(x)); }
+// the f32 forms of the GPU's training kernels (nms_learned.cu), with libm's expf
+static float softplus(float x) { return x > 0.f ? x + std::log1p(std::exp(-x)) : std::log1p(std::exp(x)); }
+static float sigmoid(float x) { return 1.f / (1.f + std::exp(-x)); }
 
-// forward (and backward when ga != nullptr) of one frame; returns the loss
-static double learned_frame(const Learned& L, const double* full_llr, const uint8_t* cw, const double* alpha,
-                            const double* beta, double* post_out, double* ga, double* gb) {
+// Forward (and backward when ga != nullptr) of one frame in arithmetic R; returns the
+// loss.  R = double is the reference arithmetic.  R = float repeats the GPU's f32
+// operations one by one (the same messages, argmins and active sets, so the adjoint takes
+// the same subgradient) and scales the loss gradient as the GPU does, by
+// 1 / (loss_bits n_frames) in f32 (`frames`); the gradients still accumulate in f64.
+template <typename R>
+static double learned_frame(const Learned& L, const R* full_llr, const uint8_t* cw, const double* alpha,
+                            const double* beta, R* post_out, double* ga, double* gb, int64_t frames = 1) {
   const Code& c = *L.c;
   const int z = c.z, rows_n = (int)L.lstart.size() - 1, T = L.T;
   const int edges = c.start.back();
-  std::vector<double> post(full_llr, full_llr + c.n), c2v(edges, 0.0);
-  std::vector<double> X((size_t)T * edges), P;
-  if (L.multi) P.assign((size_t)T * c.n, 0.0);
+  std::vector<R> post(full_llr, full_llr + c.n), c2v(edges, (R)0);
+  std::vector<R> X((size_t)T * edges), P;
+  if (L.multi) P.assign((size_t)T * c.n, (R)0);
   for (int t = 0; t < T; t++) {
     for (int Ly = 0; Ly < rows_n; Ly++)
       for (int r = 0; r < z; r++) {
         int row = Ly * z + r, d = (int)c.rows[row].size(), e0 = c.start[row];
-        double* x = &X[(size_t)t * edges + e0];
+        R* x = &X[(size_t)t * edges + e0];
         for (int i = 0; i < d; i++) x[i] = post[c.rows[row][i]] - c2v[e0 + i];
-        double sg = 1.0, m1 = INFINITY, m2 = INFINITY;
+        bool par = false;
+        R m1 = (R)INFINITY, m2 = (R)INFINITY;
         int i1 = 0;
         for (int i = 0; i < d; i++) {
-          sg *= x[i] < 0 ? -1.0 : 1.0;
-          double a = std::fabs(x[i]);
+          par ^= x[i] < 0;
+          R a = std::fabs(x[i]);
           if (a < m1) { m2 = m1; m1 = a; i1 = i; } else if (a < m2) m2 = a;
         }
         for (int i = 0; i < d; i++) {
-          double m = i == i1 ? m2 : m1, s = sg * (x[i] < 0 ? -1.0 : 1.0);
+          R m = i == i1 ? m2 : m1;
+          bool neg = par ^ (x[i] < 0);
           size_t w = widx(L, t, L.lstart[Ly] + i, r);
-          double a = alpha[w] * m - beta[w];
-          double y = s * (a > 0 ? a : 0.0);
+          R a = (R)alpha[w] * m - (R)beta[w];
+          R mag = a > 0 ? a : (R)0;
+          R y = neg ? -mag : mag;
           c2v[e0 + i] = y;
           post[c.rows[row][i]] = x[i] + y;
         }
       }
     if (L.multi) std::copy(post.begin(), post.end(), P.begin() + (size_t)t * c.n);
   }
-  auto bit_loss = [&](const double* p) {
+  auto bit_loss = [&](const R* p) {
     double l = 0.0;
-    for (int v = 0; v < L.loss_bits; v++) l += softplus(-(1.0 - 2.0 * cw[v]) * p[v]);
+    for (int v = 0; v < L.loss_bits; v++) l += (double)softplus(cw[v] ? p[v] : -p[v]);
     return l / (double)L.loss_bits;
   };
   double loss = 0.0;
@@ -946,45 +957,57 @@ static double learned_frame(const Learned& L, const double* full_llr, const uint
   if (post_out) std::copy(post.begin(), post.end(), post_out);
   if (!ga) return loss;
   // reverse sweep
-  std::vector<double> gp(c.n, 0.0), gc(edges, 0.0);
-  auto add_loss_grad = [&](const double* p, double w) {
-    for (int v = 0; v < L.loss_bits; v++) {
-      double sgn = 1.0 - 2.0 * cw[v];
-      gp[v] += -sgn * sigmoid(-sgn * p[v]) * w / (double)L.loss_bits;
+  std::vector<R> gp(c.n, (R)0), gc(edges, (R)0);
+  auto add_loss_grad = [&](const R* p, int t) {
+    if (sizeof(R) == 8) {
+      const double w = L.multi ? weight(t) : 1.0;
+      for (int v = 0; v < L.loss_bits; v++) {
+        double sgn = 1.0 - 2.0 * cw[v];
+        gp[v] += (R)(-sgn * sigmoid((double)(-sgn * p[v])) * w / (double)L.loss_bits);
+      }
+    } else {
+      const float scale = 1.f / ((float)L.loss_bits * (float)frames);
+      const float wt = L.multi == 2 ? 2.f * (float)(t + 1) / ((float)T * (float)(T + 1)) : 1.f / (float)T;
+      const float sc = L.multi ? scale * wt : scale;
+      for (int v = 0; v < L.loss_bits; v++) {
+        float sgn = cw[v] ? -1.f : 1.f;
+        gp[v] += -sgn * sigmoid((float)(-sgn * (float)p[v])) * sc;
+      }
     }
   };
-  std::vector<double> gabs(32), gy(32);
+  std::vector<R> gabs(32);
   for (int t = T - 1; t >= 0; t--) {
-    if (L.multi) add_loss_grad(&P[(size_t)t * c.n], weight(t));
-    else if (t == T - 1) add_loss_grad(post.data(), 1.0);
+    if (L.multi || t == T - 1) add_loss_grad(L.multi ? &P[(size_t)t * c.n] : post.data(), t);
     for (int Ly = rows_n - 1; Ly >= 0; Ly--)
       for (int r = 0; r < z; r++) {
         int row = Ly * z + r, d = (int)c.rows[row].size(), e0 = c.start[row];
-        const double* x = &X[(size_t)t * edges + e0];
-        double sg = 1.0, m1 = INFINITY, m2 = INFINITY;
+        const R* x = &X[(size_t)t * edges + e0];
+        bool par = false;
+        R m1 = (R)INFINITY, m2 = (R)INFINITY;
         int i1 = 0, i2 = 0;
         for (int i = 0; i < d; i++) {
-          sg *= x[i] < 0 ? -1.0 : 1.0;
-          double a = std::fabs(x[i]);
+          par ^= x[i] < 0;
+          R a = std::fabs(x[i]);
           if (a < m1) { m2 = m1; i2 = i1; m1 = a; i1 = i; } else if (a < m2) { m2 = a; i2 = i; }
         }
         if (d == 1) i2 = i1;
-        std::fill(gabs.begin(), gabs.begin() + d, 0.0);
+        std::fill(gabs.begin(), gabs.begin() + d, (R)0);
         for (int i = 0; i < d; i++) {
           int v = c.rows[row][i];
-          double m = i == i1 ? m2 : m1, s = sg * (x[i] < 0 ? -1.0 : 1.0);
+          R m = i == i1 ? m2 : m1;
+          bool neg = par ^ (x[i] < 0);
           size_t w = widx(L, t, L.lstart[Ly] + i, r);
-          double a = alpha[w] * m - beta[w];
-          double g_y = gp[v] + gc[e0 + i];
-          double g_a = a > 0 ? g_y * s : 0.0;
-          ga[w] += g_a * m;
-          gb[w] -= g_a;
-          double g_m = g_a * alpha[w];
+          R a = (R)alpha[w] * m - (R)beta[w];
+          R g_y = gp[v] + gc[e0 + i];
+          R g_a = a > 0 ? (neg ? -g_y : g_y) : (R)0;
+          ga[w] += (double)(g_a * m);
+          gb[w] -= (double)g_a;
+          R g_m = g_a * (R)alpha[w];
           gabs[i == i1 ? i2 : i1] += g_m;
         }
         for (int i = 0; i < d; i++) {
           int v = c.rows[row][i];
-          double g_x = gp[v] + (x[i] < 0 ? -1.0 : 1.0) * gabs[i];
+          R g_x = gp[v] + (x[i] < 0 ? -gabs[i] : gabs[i]);
           gp[v] = g_x;
           gc[e0 + i] = -g_x;
         }
@@ -1238,7 +1261,26 @@ double or_learned(void* h, int T, int shared, int multi, const double* alpha, co
   double tot = 0.0;
   for (int64_t f = 0; f < n; f++) {
     full_llr<double>(*c, llr + f * c->e, full.data());
-    tot += learned_frame(L, full.data(), cw + f * c->n, alpha, beta, post_out ? post_out + f * c->n : nullptr, ga, gb);
+    tot += learned_frame<double>(L, full.data(), cw + f * c->n, alpha, beta, post_out ? post_out + f * c->n : nullptr,
+                                 ga, gb);
+  }
+  return tot / (double)n;
+}
+
+// The same in the GPU's f32 arithmetic: f32 LLRs and posteriors, gradients of the mean
+// loss over the n frames (already divided by n, in f32 as the GPU scales them).
+double or_learned_f32(void* h, int T, int shared, int multi, const double* alpha, const double* beta,
+                      const float* llr, const uint8_t* cw, int64_t n, float* post_out, double* ga, double* gb,
+                      int info_only) {
+  Code* c = (Code*)h;
+  Learned L{c, T, shared != 0, {}, multi, info_only ? c->k_info : c->n};
+  learned_layers(*c, L.lstart);
+  std::vector<float> full(c->n);
+  double tot = 0.0;
+  for (int64_t f = 0; f < n; f++) {
+    full_llr<float>(*c, llr + f * c->e, full.data());
+    tot += learned_frame<float>(L, full.data(), cw + f * c->n, alpha, beta, post_out ? post_out + f * c->n : nullptr,
+                                ga, gb, n);
   }
   return tot / (double)n;
 }

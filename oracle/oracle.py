@@ -79,6 +79,8 @@ def lib():
         L.or_run_frames.argtypes = [vp, i32, u64, u64, u64, u64, u64, dbl, i32, i32, i32, vp]
         L.or_learned.restype = dbl
         L.or_learned.argtypes = [vp, i32, i32, i32, vp, vp, vp, vp, i64, vp, vp, vp, i32]
+        L.or_learned_f32.restype = dbl
+        L.or_learned_f32.argtypes = [vp, i32, i32, i32, vp, vp, vp, vp, i64, vp, vp, vp, i32]
         L.or_learned_num_weights.restype = i64
         L.or_learned_num_weights.argtypes = [vp, i32, i32]
         L.or_bpsk_frame.restype = i32
@@ -262,20 +264,26 @@ class Code:
         return out
 
     def learned(self, T, shared, alpha, beta, llr, cw, want_post=False, want_grad=False, multi=False,
-                info_only=False):
+                info_only=False, precision="f64"):
         """(mean loss, post [n x n_full] or None, (d alpha, d beta) or None) of the learned min-sum;
-        info_only: the loss over the K' information bits instead of all n_full bits."""
-        llr = np.ascontiguousarray(llr, np.float64).reshape(-1, self.e)
+        info_only: the loss over the K' information bits instead of all n_full bits;
+        precision "f32": the GPU's f32 arithmetic (same messages and argmins as the GPU)."""
+        f32 = precision == "f32"
+        rt = np.float32 if f32 else np.float64
+        llr = np.ascontiguousarray(llr, rt).reshape(-1, self.e)
         cw = np.ascontiguousarray(cw, np.uint8).reshape(-1, self.n_full)
         n = llr.shape[0]
         alpha = np.ascontiguousarray(alpha, np.float64)
         beta = np.ascontiguousarray(beta, np.float64)
-        post = np.zeros((n, self.n_full)) if want_post else None
+        post = np.zeros((n, self.n_full), rt) if want_post else None
         ga = np.zeros_like(alpha) if want_grad else None
         gb = np.zeros_like(beta) if want_grad else None
-        loss = lib().or_learned(self.h, T, int(shared), int(multi), _p(alpha), _p(beta), _p(llr), _p(cw), n, _p(post), _p(ga),
-                                _p(gb), int(bool(info_only)))
-        return loss, post, (None if ga is None else (ga / n, gb / n))
+        fn = lib().or_learned_f32 if f32 else lib().or_learned
+        loss = fn(self.h, T, int(shared), int(multi), _p(alpha), _p(beta), _p(llr), _p(cw), n, _p(post), _p(ga), _p(gb),
+                  int(bool(info_only)))
+        if ga is None:
+            return loss, post, None
+        return loss, post, ((ga, gb) if f32 else (ga / n, gb / n))
 
     def learned_num_weights(self, T, shared):
         return int(lib().or_learned_num_weights(self.h, T, int(shared)))

@@ -1,6 +1,7 @@
 """Mixed batches: every record of the persistent mixed kernel equals the single-code
 path (cb_run_frames of the item's own code on the same stream position), whatever the
-rows per thread the autotuner picks."""
+rows per thread the autotuner picks, and the oracle's f32 decoder on the LLRs the batch
+generates."""
 
 import numpy as np
 import pytest
@@ -35,6 +36,32 @@ def test_mixed_batch_equals_the_single_code_path(cb):
         assert np.array_equal(got, want), epoch
     # some frames decode, some fail, early exits differ per codeword
     assert 0 < got["frame_error"].sum() < len(items) and len(set(got["iterations"])) > 3
+
+
+def test_mixed_batch_decodes_as_the_oracle(cb, O):
+    # The oracle anchor: every item's LLRs, as the batch's generator writes them, decoded
+    # by the oracle's f32 layered min-sum (the same algorithm in f32, 25 iterations): the
+    # same iteration count and the same bit errors against the item's information bits,
+    # which are the oracle's own draws of that stream position.
+    items = cb.draw_mixed_batch(n=300, seed=5)
+    mix = cb.MixBatch(items, seed=7, name=NAME, max_iterations=25)
+    for epoch in (0, 1):
+        got = mix.run(epoch)
+        llrs, infos = mix.frames(epoch)
+        codes = {}
+        for i, it in enumerate(items):
+            key = (int(it["base_graph"]), int(it["lifting_size"]), int(it["k_info"]), int(it["e"]))
+            ref = codes.get(key)
+            if ref is None:
+                ref = codes[key] = O.Code(key[2], key[3], bg=key[0], z=key[1]).set_decoder(O.RULE_NMS, 0.75, True, 25)
+            frame = int(it["frame"]) + epoch * len(items)
+            rinfo, _, _ = ref.trial(int(it["modulation_order"]), 7, O.fnv1a64(NAME), int(it["condition"]), frame,
+                                    float(it["ebn0_db"]))
+            assert np.array_equal(infos[i], rinfo), i
+            bits, iters, _, _ = ref.decode(llrs[i], "f32")
+            assert iters == got["iterations"][i], (i, iters, got["iterations"][i])
+            assert int(np.sum(bits != rinfo)) == got["bit_errors"][i], i
+            assert bool(got["frame_error"][i]) == bool(np.any(bits != rinfo)), i
 
 
 def test_rows_per_thread_do_not_change_the_records(cb):
