@@ -65,6 +65,7 @@ SYMBOLS = [
     ("cb_code_destroy", None, [_vp]),
     ("cb_last_error", C.c_char_p, [_vp]),
     ("cb_code_set_demapper", _i32, [_vp, _i32]),
+    ("cb_code_prepare", _i32, [_vp]),
     ("cb_code_info", _i32, [_vp, _vp]),
     ("cb_code_tables", _i32, [_vp, _vp, _vp]),
     ("cb_encode", _i32, [_vp, _vp, _i64, _vp]),
@@ -204,6 +205,10 @@ class NrLdpc:
         self.precision = precision
         self.dtype = np.float64 if precision == "f64" else np.float32
         self.rule, self.alpha, self.max_iterations = rule_l, alpha, max_iterations
+
+    def prepare(self):
+        """Compile this code's decoder for its lifting into the on-disk cache (no GPU needed)."""
+        _check(lib().cb_code_prepare(self._h), self._h)
 
     DECODERS = {-1: "not yet on a device", 0: "generic layered", 1: "base-graph layered min-sum",
                 2: "layered min-sum compiled for this lifting"}

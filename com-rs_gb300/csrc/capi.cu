@@ -489,6 +489,17 @@ cb_status cb_code_set_demapper(cb_code* c, int32_t exact) {
   return CB_OK;
 }
 
+cb_status cb_code_prepare(cb_code* c) {
+  if (!c) return fail(nullptr, CB_ERR_CONFIG, "NULL code");
+  if (c->precision != CB_F32 || c->generic || !c->cfg.layered ||
+      (c->cfg.rule != cbd::RULE_NMS && c->cfg.rule != cbd::RULE_OMS))
+    return fail(c, CB_ERR_CONFIG, "only f32 layered min-sum codes run a decoder compiled for their lifting");
+  std::lock_guard<std::mutex> lock(c->mu);
+  std::string note;
+  if (!cbk::nr_prepare(c->host, &note)) return fail(c, CB_ERR_IO, "no decoder compiled for this lifting: " + note);
+  return CB_OK;
+}
+
 cb_status cb_code_info(const cb_code* c, int64_t info[16]) {
   if (!c || !info) return fail(nullptr, CB_ERR_CONFIG, "NULL argument");
   const cbh::NrCode& h = c->host;

@@ -3,16 +3,21 @@
 // Two builds of one kernel source:
 //   * compiled here by nvcc, once per base graph, with Z and the shifts read from the
 //     launch parameters: serves every code of the base graph;
-//   * compiled at run time by NVRTC for one code, with Z and every shift as constants, so
-//     that each edge address is an immediate offset and each lifted row's state address
-//     a constant: fewer instructions per edge update, the same results.  The compiled
-//     cubin is kept for the process (per base graph and lifting size) and on disk (keyed by
-//     a hash of the sources, the options and the compiler version), and loaded with the
-//     runtime's library API.  Without NVRTC, or if it fails, the nvcc build runs.
+//   * compiled at run time for one code, with Z and every shift as constants, so that
+//     each edge address is an immediate offset and each lifted row's state address a
+//     constant: fewer instructions per edge update, the same results.  The compiler is the
+//     CUDA toolkit's nvcc when one is found (its front end gives this kernel about 5 %
+//     faster code than NVRTC's, measured on GB300), else NVRTC.  The cubin is kept for the
+//     process (per base graph and lifting size) and on disk (keyed by a hash of the
+//     sources, the options and the compiler), and loaded with the runtime's library API.
+//     Without a compiler, or if it fails, the nvcc build above runs.
 #include <cuda_runtime.h>
 #include <dlfcn.h>
+#include <fcntl.h>
 #include <nvrtc.h>
+#include <spawn.h>
 #include <sys/stat.h>
+#include <sys/wait.h>
 #include <unistd.h>
 
 #include <cstdio>
@@ -23,6 +28,8 @@
 #include <sstream>
 #include <string>
 #include <vector>
+
+extern char** environ;  // passed to the compiler process
 
 #include "nr_decode.h"
 #include "nr_jit_sources.inc"  // generated by build.py: the kernel source files as text
@@ -94,6 +101,38 @@ const Nvrtc& nvrtc() {
 }
 
 const char* const kJitOptions[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--fmad=false"};
+// nvcc's, for the same code
+const char* const kNvccOptions[] = {"-cubin", "-O3", "-std=c++17", "-arch=sm_103a", "-fmad=false",
+                                    "--expt-relaxed-constexpr"};
+
+// The toolkit's nvcc: $COMRS_NVCC if set (empty: none), else $CUDA_HOME/bin/nvcc,
+// /usr/local/cuda/bin/nvcc or the first on PATH; empty when none is found or COMRS_NO_JIT
+// is set.
+const std::string& nvcc_path() {
+  static const std::string path = [] {
+    if (const char* off = std::getenv("COMRS_NO_JIT"))
+      if (*off && std::strcmp(off, "0") != 0) return std::string();
+    std::vector<std::string> cand;
+    // a set COMRS_NVCC names the compiler, or (empty) turns nvcc off: NVRTC compiles
+    if (const char* p = std::getenv("COMRS_NVCC"))
+      return std::string(*p && access(p, X_OK) == 0 ? p : "");
+    if (const char* p = std::getenv("CUDA_HOME")) cand.push_back(std::string(p) + "/bin/nvcc");
+    cand.push_back("/usr/local/cuda/bin/nvcc");
+    if (const char* p = std::getenv("PATH")) {
+      std::string s = p;
+      for (size_t a = 0; a <= s.size();) {
+        size_t b = s.find(':', a);
+        if (b == std::string::npos) b = s.size();
+        if (b > a) cand.push_back(s.substr(a, b - a) + "/nvcc");
+        a = b + 1;
+      }
+    }
+    for (const std::string& c : cand)
+      if (!c.empty() && access(c.c_str(), X_OK) == 0) return c;
+    return std::string();
+  }();
+  return path;
+}
 
 // the code's own kernel: Z and the shifts (row-major) as constants
 std::string jit_source(const cbh::NrCode& h) {
@@ -119,9 +158,17 @@ std::string cache_key(const cbh::NrCode& h, const std::string& src) {
   uint64_t k = fnv1a(0xcbf29ce484222325ull, src);
   for (int i = 0; i < kJitFileCount; i++) k = fnv1a(fnv1a(k, kJitFileNames[i]), kJitFileTexts[i]);
   for (const char* o : kJitOptions) k = fnv1a(k, o);
-  int ma = 0, mi = 0;
-  if (nvrtc().version) nvrtc().version(&ma, &mi);
-  k = fnv1a(k, std::to_string(ma) + "." + std::to_string(mi));
+  for (const char* o : kNvccOptions) k = fnv1a(k, o);
+  // the compiler: nvcc (its path and file's size and time) or NVRTC (its version)
+  const std::string& nv = nvcc_path();
+  struct stat sb;
+  if (!nv.empty() && stat(nv.c_str(), &sb) == 0) {
+    k = fnv1a(k, nv + ":" + std::to_string((long long)sb.st_size) + ":" + std::to_string((long long)sb.st_mtime));
+  } else {
+    int ma = 0, mi = 0;
+    if (nvrtc().version) nvrtc().version(&ma, &mi);
+    k = fnv1a(k, "nvrtc " + std::to_string(ma) + "." + std::to_string(mi));
+  }
   char buf[96];
   std::snprintf(buf, sizeof buf, "nr_bg%d_z%d_%016llx.cubin", h.bg, h.z, (unsigned long long)k);
   return buf;
@@ -164,7 +211,61 @@ void write_file(const std::string& dir, const std::string& name, const std::vect
   else std::remove(tmp.c_str());
 }
 
-bool compile(const cbh::NrCode& h, const std::string& src, std::vector<char>& cubin, std::string* note) {
+// nvcc on the sources written to a private temporary directory (no shell: posix_spawn)
+bool compile_nvcc(const std::string& nvcc, const std::string& src, std::vector<char>& cubin, std::string* note) {
+  const char* tmp = std::getenv("TMPDIR");
+  std::string tmpl = std::string(tmp && *tmp ? tmp : "/tmp") + "/comrs_jit_XXXXXX";
+  std::vector<char> buf(tmpl.begin(), tmpl.end());
+  buf.push_back('\0');
+  if (!mkdtemp(buf.data())) {
+    if (note) *note = "no temporary directory for nvcc";
+    return false;
+  }
+  const std::string dir = buf.data();
+  std::vector<std::string> files;
+  auto put = [&](const std::string& name, const char* text) {
+    const std::string path = dir + "/" + name;
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const size_t n = std::strlen(text);
+    const bool ok = std::fwrite(text, 1, n, f) == n;
+    std::fclose(f);
+    files.push_back(path);
+    return ok;
+  };
+  bool ok = put("nr_code.cu", src.c_str());
+  for (int i = 0; ok && i < kJitFileCount; i++) ok = put(kJitFileNames[i], kJitFileTexts[i]);
+  const std::string out = dir + "/nr_code.cubin", log = dir + "/nvcc.log", inc = "-I" + dir,
+                    in = dir + "/nr_code.cu";
+  if (ok) {
+    std::vector<const char*> argv = {nvcc.c_str()};
+    for (const char* o : kNvccOptions) argv.push_back(o);
+    for (const char* a : {inc.c_str(), in.c_str(), "-o", out.c_str()}) argv.push_back(a);
+    argv.push_back(nullptr);
+    posix_spawn_file_actions_t fa;
+    posix_spawn_file_actions_init(&fa);
+    posix_spawn_file_actions_addopen(&fa, 1, log.c_str(), O_WRONLY | O_CREAT | O_TRUNC, 0644);
+    posix_spawn_file_actions_adddup2(&fa, 1, 2);
+    pid_t pid = 0;
+    int status = 0;
+    ok = posix_spawn(&pid, nvcc.c_str(), &fa, nullptr, const_cast<char* const*>(argv.data()), environ) == 0 &&
+         waitpid(pid, &status, 0) == pid && WIFEXITED(status) && WEXITSTATUS(status) == 0;
+    posix_spawn_file_actions_destroy(&fa);
+    ok = ok && read_file(out, cubin);
+    if (!ok && note) {
+      std::vector<char> text;
+      read_file(log, text);
+      *note = "nvcc failed: " + std::string(text.begin(), text.end()).substr(0, 400);
+    }
+  }
+  files.push_back(out);
+  files.push_back(log);
+  for (const std::string& f : files) std::remove(f.c_str());
+  rmdir(dir.c_str());
+  return ok;
+}
+
+bool compile_nvrtc(const cbh::NrCode& h, const std::string& src, std::vector<char>& cubin, std::string* note) {
   const Nvrtc& api = nvrtc();
   if (!api.why.empty()) {
     if (note) *note = api.why;
@@ -193,6 +294,16 @@ bool compile(const cbh::NrCode& h, const std::string& src, std::vector<char>& cu
   }
   api.destroy(&prog);
   return ok;
+}
+
+// the code's specialisation: nvcc if found, else NVRTC
+bool compile(const cbh::NrCode& h, const std::string& src, std::vector<char>& cubin, std::string* note) {
+  const std::string& nv = nvcc_path();
+  std::string why;
+  if (!nv.empty() && compile_nvcc(nv, src, cubin, &why)) return true;
+  if (compile_nvrtc(h, src, cubin, note)) return true;
+  if (note && !why.empty()) *note = why + "; " + *note;
+  return false;
 }
 
 // the specialised kernels of this process, by cache key

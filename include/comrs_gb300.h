@@ -88,13 +88,19 @@ const char* cb_last_error(const cb_code* code);
  * log where the reference calls the platform libm. */
 cb_status cb_code_set_demapper(cb_code* code, int32_t exact);
 
+/* Compile, without a GPU, the decoder of an f32 layered min-sum code for its base graph
+ * and lifting size (Z and every shift as constants) and store it in the on-disk cache
+ * that the code's first device call reads (for build steps that warm the cache).
+ * CB_ERR_CONFIG for other codes, CB_ERR_IO when no compiler is found or it fails. */
+cb_status cb_code_prepare(cb_code* code);
+
 /* info[0..16): base graph, Z, K', E, K (systematic columns), n_full, lifted rows,
  * edges, iLS, max row degree, rv, qm, core-inverse terms, 1 if the rate matching is
  * the plain offset 2Z + t, base-graph entries, and the decoder that runs: -1 before the
  * code's first device call, 0 the generic layered decoder (f64, sum-product, flooding),
  * 1 the f32 layered min-sum built for the base graph, 2 the same compiled at run time for
- * this code's lifting size (Z and every shift as constants; needs libnvrtc, see
- * COMRS_NO_JIT and COMRS_JIT_CACHE in the integration notes). */
+ * this code's lifting size (Z and every shift as constants; needs the CUDA toolkit's nvcc
+ * or libnvrtc, see COMRS_NO_JIT, COMRS_NVCC and COMRS_JIT_CACHE in the integration notes). */
 cb_status cb_code_info(const cb_code* code, int64_t info[16]);
 
 /* The construction tables: `entries` = n_entries records (base row, base column,
