@@ -61,11 +61,12 @@ SEED, NAME = 7, "bicm_ldpc_c2"
 ALGO_BYTES = E * 4 + (K_INFO + 7) // 8 + 4
 # DRAM bytes (read + write) of the decoder per codeword at 20 iterations, and the
 # warp-instructions it issues per codeword and iteration, from one ncu capture of a
-# 2048-codeword launch (profiles/decode_c2_f32.md: 208,447,232 + 71,422,976 B,
-# smsp__inst_executed.sum = 4,894,572,480); the persistent grid keeps the same 304 state
-# slots at any batch, so both scale by codewords
-DRAM_BYTES_PER_CODEWORD = (208_447_232 + 71_422_976) / 2048
-WARP_INST_PER_CODEWORD_ITERATION = 4_894_572_480 / (2048 * 20)
+# 2048-codeword launch of the decoder compiled for this code's lifting
+# (profiles/decode_c2_f32.md: 208,589,824 + 55,173,888 B, smsp__inst_executed.sum =
+# 3,716,113,152); the persistent grid keeps the same 304 state slots at any batch, so both
+# scale by codewords
+DRAM_BYTES_PER_CODEWORD = (208_589_824 + 55_173_888) / 2048
+WARP_INST_PER_CODEWORD_ITERATION = 3_716_113_152 / (2048 * 20)
 WORKLOAD = ("5G NR LDPC BG1 Z=384 K'=8448 E=25344 (rate 1/3), Gray 16-QAM, AWGN Eb/N0 0:0.25:2 dB, "
             "max-log LLRs, layered NMS alpha=0.75, <=20 iterations + syndrome stop, 8192 codewords/launch")
 # a point at the code's waterfall (FER about 0.13; the grid above sits at FER 1)
@@ -105,7 +106,8 @@ def read_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms during the timed region
+    (the C2 bench's timed region lasts about 0.2 s)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -118,7 +120,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except Exception:
@@ -284,7 +286,7 @@ def run_ours(args, rank, world, local_rank):
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": B * DRAM_BYTES_PER_CODEWORD, "traffic_source": "ncu capture of 2048 codewords, scaled",
-                "kernel": "layered_kernel<float> (decoder)",
+                "kernel": f"layered_nr_kernel<1, ...> (decoder: {code.decoder})",
                 "algorithmic_bytes_per_launch": B * ALGO_BYTES, "launch_ms": dec,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
                 "generator_launch_ms": float(np.mean(gen_ms))}

@@ -47,6 +47,10 @@ struct cb_code {
   unsigned long long* d_counter = nullptr;
   int32_t* d_status = nullptr;
   cudaStream_t stream = nullptr;
+  // host decodes: a copy stream and, per LLR buffer, "copied" and "read by the decoder"
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_copied[2] = {nullptr, nullptr};
+  cudaEvent_t ev_read[2] = {nullptr, nullptr};
   // scratch, grown on demand
   void* d_llr = nullptr;
   size_t llr_cap = 0;
@@ -309,21 +313,35 @@ cb_status trial_device_impl(cb_code* c, int m, uint64_t seed, uint64_t name_hash
 
 template <typename T>
 cb_status decode_host_impl(cb_code* c, const T* llr, int64_t n, uint8_t* bits, T* app, int32_t* iters) {
+  // Host LLRs in chunks: chunk i + 1 is copied on the copy stream while chunk i decodes on
+  // the code's stream, through two device buffers (an event per buffer marks its copy
+  // done, another the decode that read it); decisions and counts go back on the decode
+  // stream.  Each chunk holds at least one persistent grid's worth of codewords.
   const int wpf = (c->host.k_info + 31) / 32;
   const int bpf = (c->host.k_info + 7) / 8;
-  const int64_t chunk = chunk_frames(c);
-  for (int64_t done = 0; done < n; done += chunk) {
-    int64_t cnt = std::min(chunk, n - done);
-    CB_CUDA(c, grow(c->d_llr, c->llr_cap, (size_t)cnt * c->host.e * sizeof(T)));
-    CB_CUDA(c, grow(c->d_bits, c->bits_cap, (size_t)cnt * wpf * 4));
-    if (app) CB_CUDA(c, grow(c->d_app, c->app_cap, (size_t)cnt * c->host.k_info * sizeof(T)));
-    if (iters) CB_CUDA(c, grow(c->d_iters, c->iters_cap, (size_t)cnt * 4));
-    T* d_llr = reinterpret_cast<T*>(c->d_llr);
-    CB_CUDA(c, cudaMemcpyAsync(d_llr, llr + (size_t)done * c->host.e, (size_t)cnt * c->host.e * sizeof(T),
-                               cudaMemcpyHostToDevice, c->stream));
+  const size_t per = (size_t)c->host.e * sizeof(T);
+  const int64_t grid = std::max(1, c->decode_grid);
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(chunk_frames(c) / 2,
+                                                               std::max<int64_t>(grid, (n + 3) / 4)));
+  const int64_t buf_frames = std::min(chunk, n);
+  CB_CUDA(c, grow(c->d_llr, c->llr_cap, 2 * (size_t)buf_frames * per));
+  CB_CUDA(c, grow(c->d_bits, c->bits_cap, (size_t)buf_frames * wpf * 4));
+  if (app) CB_CUDA(c, grow(c->d_app, c->app_cap, (size_t)buf_frames * c->host.k_info * sizeof(T)));
+  if (iters) CB_CUDA(c, grow(c->d_iters, c->iters_cap, (size_t)buf_frames * 4));
+  for (int64_t done = 0, i = 0; done < n; done += chunk, i++) {
+    const int64_t cnt = std::min(chunk, n - done);
+    const int half = (int)(i & 1);
+    T* d_llr = reinterpret_cast<T*>(reinterpret_cast<char*>(c->d_llr) + (size_t)half * buf_frames * per);
+    // the copy waits until the decode two chunks back has read this buffer
+    if (i >= 2) CB_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->ev_read[half], 0));
+    CB_CUDA(c, cudaMemcpyAsync(d_llr, llr + (size_t)done * c->host.e, (size_t)cnt * per, cudaMemcpyHostToDevice,
+                               c->copy_stream));
+    CB_CUDA(c, cudaEventRecord(c->ev_copied[half], c->copy_stream));
+    CB_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_copied[half], 0));
     cb_status st = decode_device_impl<T>(c, d_llr, cnt, c->d_bits, app ? reinterpret_cast<T*>(c->d_app) : nullptr,
                                          iters ? c->d_iters : nullptr, nullptr, nullptr, c->stream);
     if (st) return st;
+    CB_CUDA(c, cudaEventRecord(c->ev_read[half], c->stream));
     if (bits) {
       if (bpf == wpf * 4) {
         CB_CUDA(c, cudaMemcpyAsync(bits + (size_t)done * bpf, c->d_bits, (size_t)cnt * bpf, cudaMemcpyDeviceToHost,
@@ -356,6 +374,11 @@ cb_status ensure_device(cb_code* c) {
   cbd::DevCode& v = c->dev;
   CB_CUDA(c, cudaSetDevice(c->device));
   CB_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CB_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  for (int i = 0; i < 2; i++) {
+    CB_CUDA(c, cudaEventCreateWithFlags(&c->ev_copied[i], cudaEventDisableTiming));
+    CB_CUDA(c, cudaEventCreateWithFlags(&c->ev_read[i], cudaEventDisableTiming));
+  }
   CB_CUDA(c, cudaMalloc(&c->d_map, sizeof(int32_t) * h.e));
   CB_CUDA(c, cudaMemcpy(c->d_map, h.map.data(), sizeof(int32_t) * h.e, cudaMemcpyHostToDevice));
   CB_CUDA(c, cudaMalloc(&c->d_inv_start, sizeof(int32_t) * (h.n_full + 1)));
@@ -478,6 +501,11 @@ void cb_code_destroy(cb_code* c) {
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  for (int i = 0; i < 2; i++) {
+    if (c->ev_copied[i]) cudaEventDestroy(c->ev_copied[i]);
+    if (c->ev_read[i]) cudaEventDestroy(c->ev_read[i]);
+  }
   delete c;
 }
 

@@ -214,3 +214,17 @@ def test_concurrent_callers_on_one_code_object(cb):
     for (wb, wa, wi), (gb, ga, gi) in zip(want, got):
         assert np.array_equal(wb, gb) and np.array_equal(wi, gi)
         assert np.array_equal(wa.view(np.uint32), ga.view(np.uint32))
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_host_decode_in_chunks_equals_small_calls(cb, precision):
+    # cb_decode splits a large host batch into chunks whose copies overlap the decoding of
+    # the previous chunk; the results equal those of small calls, one chunk each
+    g = cb.NrLdpc(520, 1040, base_graph=2, lifting_size=52, precision=precision)
+    llr, _ = g.generate_frames(7, "chunks", 0, 0, 12000, 1.5, 4)
+    bits, app, it = g.decode_full(llr)
+    for a in range(0, 12000, 1500):
+        b2, a2, i2 = g.decode_full(llr[a:a + 1500])
+        assert np.array_equal(b2, bits[a:a + 1500]) and np.array_equal(i2, it[a:a + 1500])
+        assert np.array_equal(a2.view(np.uint8), app[a:a + 1500].view(np.uint8))
+    assert 0 < it.mean() < 20
