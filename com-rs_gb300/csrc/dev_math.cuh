@@ -76,6 +76,34 @@ __device__ __forceinline__ uint32_t window32(const uint32_t* col, int o) {
   return __funnelshift_r(col[o >> 5], col[(o >> 5) + 1], o & 31);
 }
 
+// Stage 2 of the syndrome test: every row on packed hard decisions.  Block-wide.
+template <typename T>
+__device__ __forceinline__ bool some_packed_check_fails(const T* post, uint32_t* hd, const uint32_t* ent,
+                                                        const uint16_t* lstart, int rows_n, int ncol, int z, int tid,
+                                                        int nt) {
+  int bad = 0;
+  build_hard_decisions(post, hd, ncol, z, tid, nt);
+  __syncthreads();
+  const int wz = (z + 31) >> 5, ws = wz + 1;
+  for (int task = tid; task < rows_n * wz && !bad; task += nt) {
+    const int L = task / wz, g = task - L * wz;
+    const int r0 = g * 32, nrows = min(32, z - r0);
+    uint32_t par = 0;
+    for (int t = lstart[L]; t < lstart[L + 1]; t++) {
+      const uint32_t en = ent[t];
+      const uint32_t* col = hd + (en >> 16) * ws;
+      int o = r0 + (int)(en & 0xffffu);
+      o -= (o >= z) ? z : 0;
+      uint32_t win = window32(col, o);
+      if (o + nrows > z) win |= window32(col, 0) << (z - o);
+      par ^= win;
+    }
+    const uint32_t mask = nrows == 32 ? 0xffffffffu : ((1u << nrows) - 1u);
+    bad = (par & mask) != 0u;
+  }
+  return __syncthreads_or(bad) != 0;
+}
+
 // Whether some check fails on the hard decisions of post (hard_decisions_are_a_codeword,
 // ldpc.rs:555-557).  Block-wide.  Stage 1 reads the rows of the first two layers
 // directly (each thread its own row, stopping at the first failure): while the
@@ -100,26 +128,7 @@ __device__ __forceinline__ bool some_check_fails(const T* post, uint32_t* hd, co
     }
   }
   if (__syncthreads_or(bad)) return true;
-  build_hard_decisions(post, hd, ncol, z, tid, nt);
-  __syncthreads();
-  const int wz = (z + 31) >> 5, ws = wz + 1;
-  for (int task = tid; task < rows_n * wz && !bad; task += nt) {
-    const int L = task / wz, g = task - L * wz;
-    const int r0 = g * 32, nrows = min(32, z - r0);
-    uint32_t par = 0;
-    for (int t = lstart[L]; t < lstart[L + 1]; t++) {
-      const uint32_t en = ent[t];
-      const uint32_t* col = hd + (en >> 16) * ws;
-      int o = r0 + (int)(en & 0xffffu);
-      o -= (o >= z) ? z : 0;
-      uint32_t win = window32(col, o);
-      if (o + nrows > z) win |= window32(col, 0) << (z - o);
-      par ^= win;
-    }
-    const uint32_t mask = nrows == 32 ? 0xffffffffu : ((1u << nrows) - 1u);
-    bad = (par & mask) != 0u;
-  }
-  return __syncthreads_or(bad) != 0;
+  return some_packed_check_fails(post, hd, ent, lstart, rows_n, ncol, z, tid, nt);
 }
 
 __device__ __forceinline__ float ld_post(const float* post, int off) {

@@ -69,7 +69,8 @@ struct NrArgs {
 };
 
 // the check-node state of a CTA: an 8-byte plane {n1, n2} and a 4-byte plane of meta words
-// (bits 0-4 an edge holding the second minimum, bits 8.. the outgoing signs)
+// (bits 0-7 the edge whose message has the second minimum's magnitude, read as bits 0-4;
+// bits 8.. the outgoing signs)
 __host__ __device__ inline size_t nr_state_bytes(int lifted_rows) {
   return (((size_t)lifted_rows * 12) + 255) & ~(size_t)255;
 }
@@ -90,13 +91,33 @@ struct RuntimeLifting {
   static constexpr int shift[1] = {0};
 };
 
+// Per lifting policy (all choices give the same results; measured on GB300):
+//   ahead        how many rows ahead of its update a row's check-node state is loaded
+//                (0: at the row's start).  Fixed lifting: two (C2, 8192 codewords: 15.32
+//                ms, one: 15.53, none: 16.1).  Runtime lifting: the extra registers make
+//                the kernel spill, so none.
+//   fixed_stage1 stage 1 of the syndrome test with the base graph's first two rows at
+//                compile time, instead of read from the entry table.
+//   mad_select   the output magnitude chosen by an integer multiply-add (nr_row).
+template <class K>
+struct NrTuning {
+  static constexpr int ahead = K::fixed ? 2 : 0;
+  static constexpr bool fixed_stage1 = K::fixed;
+  static constexpr bool mad_select = K::fixed;
+};
+
 // Byte offset in the posteriors of entry T's variable for lifted row r (r4 = 4 r):
-// 4 (column Z + (r + shift) mod Z).
+// 4 (column Z + (r + shift) mod Z).  Since r + shift < 2Z, the residue is the unsigned
+// minimum of u = 4 (r + shift) and u - 4Z (one `viaddmin`); with a fixed lifting the
+// column's offset is an immediate of the shared-memory access.  (A comparison of r with
+// Z - shift selecting between two immediates issues more instructions: 17.6 against
+// 16.7 ms per 8192 C2 codewords.)
 template <int BG, class K, int T>
 __device__ __forceinline__ int edge_offset(const NrArgs& a, int r, int r4, int z4) {
   if constexpr (K::fixed) {
     constexpr int sh = K::shift[T], c = Graph<BG>::col[T];
-    return r >= K::z - sh ? r4 + 4 * (c * K::z + sh - K::z) : r4 + 4 * (c * K::z + sh);
+    const uint32_t u = (uint32_t)r4 + (uint32_t)(4 * sh);
+    return 4 * c * K::z + (int)__viaddmin_u32(u, (uint32_t)(-4 * K::z), u);
   } else {
     // r + shift < 2Z: (r + shift) mod Z is the unsigned minimum of u and u - Z
     const uint2 t = a.eaddr[T];
@@ -162,18 +183,34 @@ __device__ __forceinline__ void nr_row(unsigned char* post, const NrArgs& a, int
     n2 = fmaxf(__fsub_rn(m2, alpha), 0.0f);
   }
   const uint32_t n1p = __float_as_uint(n1) | ps, n2p = __float_as_uint(n2) | ps;
-  uint32_t sm = 0;
-  int i1 = 0;
+  // Each edge's magnitude is n2 where |x| equals the minimum, else n1.  The choice is an
+  // integer multiply-add by the comparison's mask (0 or all ones), which runs on the FMA
+  // pipe beside the ALU-bound rest (14.5 against 15.2 ms per 8192 C2 codewords with two
+  // selects).  The same multiply-add sums the indices of those edges: when one edge holds
+  // the minimum the sum is its index; when several tie, m1 = m2, the two magnitudes of
+  // the state are equal and any index gives the same old messages.  The sum (at most
+  // 0 + 1 + ... + 18) stays below the sign bits at bit 8.
+  // (With NrTuning::mad_select off: two selects, the last such edge's index.)
+  const uint32_t dneg = n1p - n2p;
+  uint32_t sm = 0, i1 = 0;
 #pragma unroll
   for (int i = 0; i < D; i++) {
-    const bool eq = fabsf(x[i]) == m1;
-    const uint32_t magp = eq ? n2p : n1p;
-    i1 = eq ? i : i1;
+    uint32_t magp;
+    if constexpr (NrTuning<K>::mad_select) {
+      uint32_t eqm;
+      asm("set.eq.u32.f32 %0, %1, %2;" : "=r"(eqm) : "f"(fabsf(x[i])), "f"(m1));
+      asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(magp) : "r"(eqm), "r"(dneg), "r"(n1p));
+      if (i) asm("mad.lo.u32 %0, %1, %2, %0;" : "+r"(i1) : "r"(eqm), "r"((uint32_t)-i));
+    } else {
+      const bool eq = fabsf(x[i]) == m1;
+      magp = eq ? n2p : n1p;
+      i1 = eq ? (uint32_t)i : i1;
+    }
     const uint32_t ob = magp ^ (__float_as_uint(x[i]) & 0x80000000u);
     st_f(post, off[i], __fadd_rn(x[i], __uint_as_float(ob)));
     sm = (sm << 1) | (ob >> 31);
   }
-  nm = (sm << 8) | (uint32_t)i1;
+  nm = (sm << 8) | i1;
 }
 
 struct NrState {
@@ -199,30 +236,75 @@ struct NrState {
   }
 };
 
-// One layered iteration: the rows in schedule order, a barrier after each level.
+// One layered iteration: the rows in schedule order, a barrier after each level.  With
+// NrTuning::ahead = 2 the state of row Q arrives as a*, that of row Q + 1 as b*, and row
+// Q + 2's is loaded here (c*), so that the L2 latency of the loads is not the first wait
+// of every row; with ahead = 0 each row loads its own state.
 template <int BG, class K, int Q>
 __device__ __forceinline__ void nr_iteration(unsigned char* post, const NrArgs& a, const NrState& st, int r, int r4,
-                                             int z4, int z, bool active, bool first, bool nms, float alpha) {
+                                             int z4, int z, bool active, bool first, bool nms, float alpha, float a1,
+                                             float a2, uint32_t mt, float b1, float b2, uint32_t bt) {
   if constexpr (Q < Graph<BG>::rows) {
     constexpr int L = Graph<BG>::order[Q];
     constexpr int S0 = Graph<BG>::start[L];
     constexpr int D = Graph<BG>::start[L + 1] - S0;
+    constexpr int ahead = NrTuning<K>::ahead;
+    const int zz = K::fixed ? K::z : z;
+    float c1 = 0.0f, c2 = 0.0f;
+    uint32_t ct = 0;
+    if constexpr (ahead == 2 && Q + 2 < Graph<BG>::rows) {
+      if (active && !first) st.load(Graph<BG>::order[Q + 2] * zz + r, c1, c2, ct);
+    }
     if (active) {
       // the row index passes through an empty asm so that the compiler recomputes each
       // row's addresses where they are used instead of hoisting all of them out of the
       // iteration loop (they would not fit in registers)
       int rr = r, rr4 = r4;
       asm volatile("" : "+r"(rr), "+r"(rr4));
-      const int zz = K::fixed ? K::z : z;
-      float a1 = 0.0f, a2 = 0.0f, n1, n2;
-      uint32_t mt = 0, nm;
-      if (!first) st.load(L * zz + rr, a1, a2, mt);
+      if constexpr (ahead == 0) {
+        if (!first) st.load(L * zz + rr, a1, a2, mt);
+      }
+      float n1, n2;
+      uint32_t nm;
       nr_row<BG, K, S0, D>(post, a, rr, rr4, z4, a1, a2, mt, nms, alpha, n1, n2, nm);
       st.store(L * zz + rr, n1, n2, nm);
     }
     if constexpr (Graph<BG>::level_end[Q] != 0) __syncthreads();
-    nr_iteration<BG, K, Q + 1>(post, a, st, r, r4, z4, z, active, first, nms, alpha);
+    nr_iteration<BG, K, Q + 1>(post, a, st, r, r4, z4, z, active, first, nms, alpha, b1, b2, bt, c1, c2, ct);
   }
+}
+
+// the parity (sign bits of the hard decisions) of lifted row r of base row L: entries
+// T .. TE - 1 at compile time
+template <int BG, class K, int T, int TE>
+__device__ __forceinline__ uint32_t row_parity(const unsigned char* post, const NrArgs& a, int r, int r4, int z4) {
+  if constexpr (T < TE) {
+    return (uint32_t)(ld_f(post, edge_offset<BG, K, T>(a, r, r4, z4)) < 0.0f) ^
+           row_parity<BG, K, T + 1, TE>(post, a, r, r4, z4);
+  } else {
+    return 0u;
+  }
+}
+
+// some_check_fails (dev_math.cuh) with stage 1, the rows of the first two base rows, at
+// compile time: the same answer, exactly "H c != 0"
+template <int BG, class K>
+__device__ __forceinline__ bool some_nr_check_fails(const float* post, uint32_t* hd, const uint32_t* ent,
+                                                    const uint16_t* lstart, const NrArgs& a, int ncol, int z, int tid,
+                                                    int nt, int r4, int z4) {
+  if constexpr (!NrTuning<K>::fixed_stage1) {
+    return some_check_fails(post, hd, ent, lstart, a.rows, ncol, z, tid, nt);
+  }
+  int bad = 0;
+  if (tid < z) {
+    int rr = tid, rr4 = r4;
+    asm volatile("" : "+r"(rr), "+r"(rr4));
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(post);
+    bad = (int)row_parity<BG, K, Graph<BG>::start[0], Graph<BG>::start[1]>(p, a, rr, rr4, z4);
+    if (!bad) bad = (int)row_parity<BG, K, Graph<BG>::start[1], Graph<BG>::start[2]>(p, a, rr, rr4, z4);
+  }
+  if (__syncthreads_or(bad)) return true;
+  return some_packed_check_fails(post, hd, ent, lstart, a.rows, ncol, z, tid, nt);
 }
 
 // Persistent kernel: each CTA takes codewords from the work counter, one thread per
@@ -297,12 +379,22 @@ __global__ void __launch_bounds__(384, 2) layered_nr_kernel(const __grid_constan
 
     // ---- propagate (ldpc.rs:509-551): syndrome test before the first iteration and after each
     int it = 0;
+    // (the test before the first iteration, once per codeword, runs the table-driven
+    // stage 1: with the compile-time one here too the kernel spills registers)
     if (some_check_fails(post, hd, s_ent, s_lstart, a.rows, ncol, z, tid, nt)) {
       it = max_it;
       for (int iter = 1; iter <= max_it; iter++) {
+        float a1 = 0.0f, a2 = 0.0f, b1 = 0.0f, b2 = 0.0f;
+        uint32_t mt = 0, bt = 0;
+        if constexpr (NrTuning<K>::ahead == 2) {
+          if (active && iter != 1) {
+            st.load(Graph<BG>::order[0] * z + tid, a1, a2, mt);
+            st.load(Graph<BG>::order[1] * z + tid, b1, b2, bt);
+          }
+        }
         nr_iteration<BG, K, 0>(reinterpret_cast<unsigned char*>(post), a, st, tid, r4, z4, z, active, iter == 1, nms,
-                               alpha);
-        if (!some_check_fails(post, hd, s_ent, s_lstart, a.rows, ncol, z, tid, nt)) {
+                               alpha, a1, a2, mt, b1, b2, bt);
+        if (!some_nr_check_fails<BG, K>(post, hd, s_ent, s_lstart, a, ncol, z, tid, nt, r4, z4)) {
           it = iter;
           break;
         }
