@@ -91,19 +91,14 @@ struct RuntimeLifting {
   static constexpr int shift[1] = {0};
 };
 
-// Per lifting policy (all choices give the same results; measured on GB300):
-//   ahead        how many rows ahead of its update a row's check-node state is loaded
-//                (0: at the row's start).  Fixed lifting: two (C2, 8192 codewords: 15.32
-//                ms, one: 15.53, none: 16.1).  Runtime lifting: the extra registers make
-//                the kernel spill, so none.
-//   fixed_stage1 stage 1 of the syndrome test with the base graph's first two rows at
-//                compile time, instead of read from the entry table.
-//   mad_select   the output magnitude chosen by an integer multiply-add (nr_row).
+// How many rows ahead of its update a row's check-node state is loaded (0: at the row's
+// start), per lifting policy; the results are the same.  Fixed lifting: two (C2, 8192
+// codewords on GB300: 15.32 ms, one row ahead 15.53, none 16.1, before the multiply-add
+// output choice).  Runtime lifting: the registers of the loads in flight make that
+// kernel spill (23.5 ms with two rows ahead, 17.4 with none).
 template <class K>
 struct NrTuning {
   static constexpr int ahead = K::fixed ? 2 : 0;
-  static constexpr bool fixed_stage1 = K::fixed;
-  static constexpr bool mad_select = K::fixed;
 };
 
 // Byte offset in the posteriors of entry T's variable for lifted row r (r4 = 4 r):
@@ -190,22 +185,15 @@ __device__ __forceinline__ void nr_row(unsigned char* post, const NrArgs& a, int
   // the minimum the sum is its index; when several tie, m1 = m2, the two magnitudes of
   // the state are equal and any index gives the same old messages.  The sum (at most
   // 0 + 1 + ... + 18) stays below the sign bits at bit 8.
-  // (With NrTuning::mad_select off: two selects, the last such edge's index.)
+  // (The runtime-lifting build: 17.4 against 18.6 ms.)
   const uint32_t dneg = n1p - n2p;
   uint32_t sm = 0, i1 = 0;
 #pragma unroll
   for (int i = 0; i < D; i++) {
-    uint32_t magp;
-    if constexpr (NrTuning<K>::mad_select) {
-      uint32_t eqm;
-      asm("set.eq.u32.f32 %0, %1, %2;" : "=r"(eqm) : "f"(fabsf(x[i])), "f"(m1));
-      asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(magp) : "r"(eqm), "r"(dneg), "r"(n1p));
-      if (i) asm("mad.lo.u32 %0, %1, %2, %0;" : "+r"(i1) : "r"(eqm), "r"((uint32_t)-i));
-    } else {
-      const bool eq = fabsf(x[i]) == m1;
-      magp = eq ? n2p : n1p;
-      i1 = eq ? (uint32_t)i : i1;
-    }
+    uint32_t eqm, magp;
+    asm("set.eq.u32.f32 %0, %1, %2;" : "=r"(eqm) : "f"(fabsf(x[i])), "f"(m1));
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(magp) : "r"(eqm), "r"(dneg), "r"(n1p));
+    if (i) asm("mad.lo.u32 %0, %1, %2, %0;" : "+r"(i1) : "r"(eqm), "r"((uint32_t)-i));
     const uint32_t ob = magp ^ (__float_as_uint(x[i]) & 0x80000000u);
     st_f(post, off[i], __fadd_rn(x[i], __uint_as_float(ob)));
     sm = (sm << 1) | (ob >> 31);
@@ -287,14 +275,12 @@ __device__ __forceinline__ uint32_t row_parity(const unsigned char* post, const 
 }
 
 // some_check_fails (dev_math.cuh) with stage 1, the rows of the first two base rows, at
-// compile time: the same answer, exactly "H c != 0"
+// compile time: the same answer, exactly "H c != 0" (C2 on GB300, runtime lifting: 18.2
+// against 18.6 ms per 8192 codewords)
 template <int BG, class K>
 __device__ __forceinline__ bool some_nr_check_fails(const float* post, uint32_t* hd, const uint32_t* ent,
                                                     const uint16_t* lstart, const NrArgs& a, int ncol, int z, int tid,
                                                     int nt, int r4, int z4) {
-  if constexpr (!NrTuning<K>::fixed_stage1) {
-    return some_check_fails(post, hd, ent, lstart, a.rows, ncol, z, tid, nt);
-  }
   int bad = 0;
   if (tid < z) {
     int rr = tid, rr4 = r4;
