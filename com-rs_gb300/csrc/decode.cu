@@ -191,17 +191,22 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
     // of decisions are staged in hd (free after the syndrome test) and written 16 bytes at
     // a time when the row of words allows it.
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-    unsigned int be = 0;
+    // the sent words, one per thread, loaded before the ballots so that their latency
+    // overlaps them
+    const uint32_t* ref = a.ref_bits ? a.ref_bits + (size_t)cw * wpf : nullptr;
+    const uint32_t ref_w = (ref && tid < wpf) ? ref[tid] : 0u;
     for (int b0 = warp * 32; b0 < c.k_info; b0 += nw * 32) {
       int v = b0 + lane;
       bool bit = v < c.k_info && post[v] < (T)0;
       uint32_t word = __ballot_sync(0xffffffffu, bit);
-      if (lane == 0) {
-        hd[b0 >> 5] = word;
-        if (a.ref_bits) be += __popc(word ^ a.ref_bits[(size_t)cw * wpf + (b0 >> 5)]);
-      }
+      if (lane == 0) hd[b0 >> 5] = word;
     }
     __syncthreads();
+    unsigned int be = 0;
+    if (ref) {
+      if (tid < wpf) be = __popc(hd[tid] ^ ref_w);
+      for (int w = tid + nt; w < wpf; w += nt) be += __popc(hd[w] ^ ref[w]);
+    }
     if (a.bits_out) {
       uint32_t* dst = a.bits_out + (size_t)cw * wpf;
       if ((wpf & 3) == 0 && (reinterpret_cast<uintptr_t>(a.bits_out) & 15) == 0) {
