@@ -367,6 +367,10 @@ def run_ours(args, rank, world, local_rank):
     # decoder's own code (benchmark config 5) with the protocol's committed weights
     decoders, _, _, _ = learned_decoders("c5", 2, 1, world, rank, local_rank, barrier, max_over_ranks)
 
+    # the batched uneven mix (benchmark config 3) through its public API, so that the default
+    # line carries it too (`--workload mix` measures it with its roofline and CPU baseline)
+    mix = mix_summary(local_rank, rank, world, barrier, max_over_ranks)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         gbps, cores, n, frames, t, _ = cpu_sample(2, 0, budget_s=5.0)
@@ -378,7 +382,7 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0:
         config = c2_config(world, B)
         config.update({"last_step_fer": fer_acc[-1], "last_step_mean_iterations": it_acc[-1],
-                       "waterfall": waterfall, "decoders": decoders})
+                       "waterfall": waterfall, "decoders": decoders, "mix": mix})
         line = {"metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (Monte Carlo frames from seeded streams)",
@@ -630,6 +634,35 @@ def mix_cpu_sample(budget_s, threads=0):
             done += n
     t = time.perf_counter() - t0
     return bits / t / 1e9, cores, done, t
+
+
+def mix_summary(local_rank, rank, world, barrier, max_over_ranks, replays=3):
+    """The mixed batch's throughput for the default line: autotuned, two warm-up replays,
+    then `replays` replays timed on the host clock (device work and the records), and the
+    decode phase alone event-timed inside the library."""
+    cb = importlib.import_module("com-rs_gb300")
+    items = cb.draw_mixed_batch(n=MIX_N, seed=MIX_ITEMS_SEED)
+    mix = cb.MixBatch(items, seed=MIX_SEED, name=MIX_NAME, max_iterations=25, device=local_rank)
+    try:
+        tuned = cb.autotune(mix, reps=2, cache=False)
+        bits = int(items["k_info"].sum())
+        for s in range(2):
+            mix.run(epoch=20_000 + s)
+        barrier()
+        fer = []
+        t0 = time.perf_counter()
+        for s in range(replays):
+            rec = mix.run(epoch=s * world + rank)
+            fer.append(float(rec["frame_error"].mean()))
+        barrier()
+        wall = max_over_ranks(time.perf_counter() - t0)
+        dec_ms = mix.time_decode(-1, reps=3)
+    finally:
+        mix.close()
+    return {"workload": MIX_WORKLOAD, "value": replays * world * bits / wall / 1e9, "unit": "Gbit/s",
+            "ms_per_replay": wall / replays * 1e3, "decode_phase_ms": dec_ms, "mean_fer": float(np.mean(fer)),
+            "codewords_per_replay": MIX_N, "rows_per_thread": {str(z): v[0] for z, v in tuned.items()},
+            "timing": "host clock around the synchronous replay call (cb_mix_run: generator, decoder, records)"}
 
 
 def run_mix_reference(args, rank):

@@ -200,7 +200,7 @@ cb_status gen_config(cb_code* c, int m, GenCache** out) {
   GenCache g;
   if (!cbh::qam_points(m, g.points, g.log_m)) return fail(c, CB_ERR_CONFIG, "modulation order must be 4, 16, 64 or 256");
   g.m = m;
-  const cbh::GenTables t = cbh::gen_tables(c->host.k_info, c->host.e, m, cbk::kGenThreads);
+  const cbh::GenTables t = cbh::gen_tables(c->host.k_info, c->host.e, m, cbk::kGenBitsThreads, cbk::kGenNoiseThreads);
   g.mbits = t.mbits;
   g.n_pad = t.n_pad;
   g.bpc = t.bits_per_chunk;

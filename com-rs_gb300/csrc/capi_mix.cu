@@ -232,7 +232,8 @@ cb_status cb_mix_create(const cb_mix_item* items, int64_t n, uint64_t seed, uint
       }
       gid = (int)tables.size();
       config_id[ck] = gid;
-      tables.push_back(cbh::gen_tables(m->codes[cid].k_info, m->codes[cid].e, d.modulation_order, cbk::kGenThreads));
+      tables.push_back(cbh::gen_tables(m->codes[cid].k_info, m->codes[cid].e, d.modulation_order, cbk::kGenBitsThreads,
+                                       cbk::kGenNoiseThreads));
       points.push_back(pts);
       log_m.push_back(lm);
       mods.push_back(d.modulation_order);

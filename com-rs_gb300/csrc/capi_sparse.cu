@@ -699,7 +699,8 @@ cb_status cb_link_create(cb_ldpc* code, int32_t blocks, int32_t modulation_order
     delete l;
     return kfail(nullptr, CB_ERR_CONFIG, "modulation order must be 4, 16, 64 or 256");
   }
-  const cbh::GenTables t = cbh::gen_tables(code->enc.k * blocks, (int)nb, modulation_order, cbk::kGenThreads);
+  const cbh::GenTables t = cbh::gen_tables(code->enc.k * blocks, (int)nb, modulation_order, cbk::kGenThreads,
+                                            cbk::kGenThreads);
   l->mbits = t.mbits;
   l->n_pad = t.n_pad;
   l->bpc = t.bits_per_chunk;

@@ -282,27 +282,27 @@ bool qam_points(int m, std::vector<double>& pts, double& log_m) {
   return true;
 }
 
-GenTables gen_tables(int k_info, int e, int m, int threads) {
+GenTables gen_tables(int k_info, int e, int m, int bits_threads, int noise_threads) {
   GenTables g;
   g.mbits = __builtin_ctz(m);
   g.n_pad = (g.mbits - e % g.mbits) % g.mbits;
   int n_sym = (e + g.n_pad) / g.mbits;
-  g.bits_per_chunk = (k_info + threads - 1) / threads;
-  g.syms_per_chunk = (n_sym + threads - 1) / threads;
-  g.jumps.assign((size_t)(2 * threads + 1) * 4, 0);
+  g.bits_per_chunk = (k_info + bits_threads - 1) / bits_threads;
+  g.syms_per_chunk = (n_sym + noise_threads - 1) / noise_threads;
+  g.jumps.assign((size_t)(bits_threads + noise_threads + 1) * 4, 0);
   JumpPoly step_b = xoshiro_jump_poly((uint64_t)g.bits_per_chunk), cur = xoshiro_jump_poly(0);
-  for (int t = 0; t < threads; t++) {
+  for (int t = 0; t < bits_threads; t++) {
     std::memcpy(&g.jumps[(size_t)t * 4], cur.w, 32);
     cur = xoshiro_jump_mul(cur, step_b);
   }
   JumpPoly step_s = xoshiro_jump_poly(2ull * g.syms_per_chunk);
   cur = xoshiro_jump_poly((uint64_t)k_info + g.n_pad);
-  for (int t = 0; t < threads; t++) {
-    std::memcpy(&g.jumps[(size_t)(threads + t) * 4], cur.w, 32);
+  for (int t = 0; t < noise_threads; t++) {
+    std::memcpy(&g.jumps[(size_t)(bits_threads + t) * 4], cur.w, 32);
     cur = xoshiro_jump_mul(cur, step_s);
   }
   JumpPoly padp = xoshiro_jump_poly((uint64_t)k_info);
-  std::memcpy(&g.jumps[(size_t)(2 * threads) * 4], padp.w, 32);
+  std::memcpy(&g.jumps[(size_t)(bits_threads + noise_threads) * 4], padp.w, 32);
   return g;
 }
 

@@ -75,6 +75,10 @@ struct GenTables {
   int mbits = 0, n_pad = 0, bits_per_chunk = 0, syms_per_chunk = 0;
   std::vector<uint64_t> jumps;
 };
-GenTables gen_tables(int k_info, int e, int m, int threads);
+// Chunks of a frame's draws: the K' information bits over `bits_threads` threads, the
+// noise symbols over `noise_threads`; jumps holds the jump polynomials of the bit chunks'
+// starts, then of the noise chunks' starts, then of the padding bits' start (after the
+// information bits).
+GenTables gen_tables(int k_info, int e, int m, int bits_threads, int noise_threads);
 
 }  // namespace cbh

@@ -170,18 +170,23 @@ __device__ __forceinline__ void row_update_lean(float* __restrict__ post, const 
     n2 = fmaxf(__fsub_rn(m2, alpha), 0.0f);
   }
   const uint32_t n1p = __float_as_uint(n1) | ps, n2p = __float_as_uint(n2) | ps;
-  uint32_t sm = 0;
-  int i1 = 0;
+  // n2 where |x| equals the minimum, else n1, by an integer multiply-add with the
+  // comparison's mask (0 or all ones) on the FMA pipe; a second one sums the indices of
+  // those edges: one edge's index when the minimum is unique; when several tie, m1 = m2
+  // and any index gives the same old messages (the sum, at most 171, stays below bit 8)
+  const uint32_t dneg = n1p - n2p;
+  uint32_t sm = 0, i1 = 0;
 #pragma unroll
   for (int e = 0; e < D; e++) {
-    const bool eq = fabsf(x[e]) == m1;
-    const uint32_t magp = eq ? n2p : n1p;
-    i1 = eq ? e : i1;
+    uint32_t eqm, magp;
+    asm("set.eq.u32.f32 %0, %1, %2;" : "=r"(eqm) : "f"(fabsf(x[e])), "f"(m1));
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(magp) : "r"(eqm), "r"(dneg), "r"(n1p));
+    if (e) asm("mad.lo.u32 %0, %1, %2, %0;" : "+r"(i1) : "r"(eqm), "r"((uint32_t)-e));
     const uint32_t ob = magp ^ (__float_as_uint(x[e]) & 0x80000000u);
     st_post(post, off[e], __fadd_rn(x[e], __uint_as_float(ob)));
     sm = (sm << 1) | (ob >> 31);
   }
-  nm = (sm << 8) | (uint32_t)i1;
+  nm = (sm << 8) | i1;
 }
 
 // The learned min-sum's weights of one row: alpha and beta of the previous and the

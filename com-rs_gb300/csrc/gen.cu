@@ -6,7 +6,8 @@
 // (source::bits, crates/com-mapping/src/source.rs:30-32, Rng::bit rng.rs:146-148); the
 // padding bits of map (blocks/coding/map.rs:36-38); then two uniforms per symbol for
 // its complex Gaussian (rng.rs:161-167).  The draws are split over the CTA's threads in
-// contiguous chunks; each thread reaches its chunk's start with a xoshiro256**
+// contiguous chunks (the bits over the first warp, the noise over the other three); each
+// thread reaches its chunk's start with a xoshiro256**
 // jump-ahead polynomial (the state after n steps is P_n(T) s, P_n = x^n mod the
 // characteristic polynomial of the transition T), so every value equals the
 // sequential draw.
@@ -133,19 +134,22 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
   const uint64_t fidx = a.frame_index;
 
   for (int i = tid; i < 2 * a.m; i += NT) pts[i] = a.points[i];
-  // ---- info bits: chunk [tid * bpc, (tid + 1) * bpc)
-  {
-    cbd::Xoshiro r = cbd::stream(a.seed, a.name_hash, a.cond, fidx);
-    int b0 = tid * a.bits_per_chunk, b1 = min(b0 + a.bits_per_chunk, c.k_info);
+  // ---- info bits by the first warp, thread t the chunk [t bpc, (t + 1) bpc); the thread
+  // whose chunk ends at K' draws the padding bits next, as they follow the info bits.
+  // Meanwhile each thread of the other warps jumps to the start of its noise chunk
+  // (symbols [(t - BT) spc, ...)), which it draws after the encoding.
+  constexpr int BT = kGenBitsThreads;
+  cbd::Xoshiro rn = cbd::stream(a.seed, a.name_hash, a.cond, fidx);
+  if (tid < BT) {
+    const int b0 = tid * a.bits_per_chunk, b1 = min(b0 + a.bits_per_chunk, c.k_info);
     if (b0 < b1) {
-      cbd::xoshiro_jump(r, a.jumps + 4 * tid);
-      for (int i = b0; i < b1; i++) cw[i] = (uint8_t)(cbd::xoshiro_next(r) >> 63);
+      cbd::xoshiro_jump(rn, a.jumps + 4 * tid);
+      for (int i = b0; i < b1; i++) cw[i] = (uint8_t)(cbd::xoshiro_next(rn) >> 63);
+      if (b1 == c.k_info)
+        for (int i = 0; i < a.n_pad; i++) pad[i] = (uint8_t)(cbd::xoshiro_next(rn) >> 63);
     }
-    if (tid == 0 && a.n_pad) {  // the padding bits follow the info bits
-      cbd::Xoshiro p = cbd::stream(a.seed, a.name_hash, a.cond, fidx);
-      cbd::xoshiro_jump(p, a.jumps + 4 * (2 * NT));
-      for (int i = 0; i < a.n_pad; i++) pad[i] = (uint8_t)(cbd::xoshiro_next(p) >> 63);
-    }
+  } else if ((tid - BT) * a.syms_per_chunk < n_sym) {
+    cbd::xoshiro_jump(rn, a.jumps + 4 * tid);
   }
   for (int i = c.k_info + tid; i < c.n_full; i += NT) cw[i] = 0;
   __syncthreads();
@@ -276,11 +280,12 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
   }
   __syncthreads();
   const double sigma2 = s_sigma2;
-  // ---- noise and demapping, symbol chunk [tid * spc, (tid + 1) * spc)
-  int s0 = tid * a.syms_per_chunk, s1 = min(s0 + a.syms_per_chunk, n_sym);
+  // ---- noise and demapping by the threads past the first warp, symbol chunk
+  // [(tid - BT) spc, (tid - BT + 1) spc), from the state they jumped to
+  if (tid < BT) return;
+  int s0 = (tid - BT) * a.syms_per_chunk, s1 = min(s0 + a.syms_per_chunk, n_sym);
   if (s0 >= s1) return;
-  cbd::Xoshiro r = cbd::stream(a.seed, a.name_hash, a.cond, fidx);
-  cbd::xoshiro_jump(r, a.jumps + 4 * (NT + tid));
+  cbd::Xoshiro& r = rn;
   T* out = a.llr_out;
   if (sizeof(T) == 8) {
     const double sd = __dsqrt_rn(sigma2);

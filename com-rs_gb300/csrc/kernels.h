@@ -59,7 +59,7 @@ struct GenArgs {
   double b_ebn0;               // (log2 M * R) * db2lin(Eb/N0), computed on the host
   uint64_t seed, name_hash, cond, first_frame;
   int64_t n_frames;
-  const uint64_t* jumps;       // [2 * threads][4]: jump polynomials of the chunk starts
+  const uint64_t* jumps;       // [bits + noise threads + 1][4]: jump polynomials of the chunk starts
   int32_t bits_per_chunk, syms_per_chunk, n_pad;
   T* llr_out;                  // [n_frames][E]
   uint32_t* info_out;          // [n_frames][ceil(K'/32)]
@@ -71,6 +71,12 @@ struct GenArgs {
   int32_t exact = 0;           // demapper: 1 Jacobian::Exact (log-sum-exp), 0 max-log
 };
 constexpr int kGenThreads = 128;
+// The NR frame generator (gen_one) draws the information bits with its first warp and the
+// noise with the other three, whose threads jump to their noise chunks while the first
+// warp draws the bits: 128 jumps a frame instead of 256 (a jump costs about 256 steps of
+// the generator, four times a bit chunk's own draws).
+constexpr int kGenBitsThreads = 32;
+constexpr int kGenNoiseThreads = kGenThreads - kGenBitsThreads;
 
 // The generation parameters of one frame (everything but the code).
 template <typename T>

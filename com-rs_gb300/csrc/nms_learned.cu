@@ -284,12 +284,20 @@ __global__ void __launch_bounds__(384) learned_forward_kernel(const __grid_const
   }
   const int wpf = (c.k_info + 31) >> 5, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   unsigned int be = 0;
-  if (a.ref_bits)
+  // the sent words, one per thread, loaded before the ballots so that their latency
+  // overlaps them; the decisions are staged in hd (free after the syndrome tests)
+  const uint32_t* ref = a.ref_bits ? a.ref_bits + (size_t)f * wpf : nullptr;
+  const uint32_t ref_w = (ref && tid < wpf) ? ref[tid] : 0u;
+  if (ref) {
     for (int b0 = warp * 32; b0 < c.k_info; b0 += nw * 32) {
       int v = b0 + lane;
       uint32_t word = __ballot_sync(0xffffffffu, v < c.k_info && post[v] < 0.f);
-      if (lane == 0) be += __popc(word ^ a.ref_bits[(size_t)f * wpf + (b0 >> 5)]);
+      if (lane == 0) hd[b0 >> 5] = word;
     }
+    __syncthreads();
+    if (tid < wpf) be = __popc(hd[tid] ^ ref_w);
+    for (int w = tid + nt; w < wpf; w += nt) be += __popc(hd[w] ^ ref[w]);
+  }
   if (be) atomicAdd(&s_err, be);
   __syncthreads();
   if (tid == 0) {
