@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <mutex>
 #include <string>
@@ -525,6 +526,8 @@ cb_status cb_code_prepare(cb_code* c) {
   std::lock_guard<std::mutex> lock(c->mu);
   std::string note;
   if (!cbk::nr_prepare(c->host, &note)) return fail(c, CB_ERR_IO, "no decoder compiled for this lifting: " + note);
+  if (!cbk::nr_prepare(c->host, &note, true))
+    return fail(c, CB_ERR_IO, "no learned decoder compiled for this lifting: " + note);
   return CB_OK;
 }
 
@@ -690,6 +693,10 @@ cb_status cb_xoshiro_jump(const uint64_t state[4], uint64_t steps, uint64_t out[
 struct cb_nms {
   cb_code* code = nullptr;
   int T = 0, shared = 0, step = 0;
+  // evaluation on the graph-specialised decoder (layered_nr_kernel with NrLearnedArgs):
+  // its kernel and grid (0: not usable, -1: not yet looked at)
+  cbk::NrKernel nr;
+  int nr_grid = -1;
   int info_only_loss = 0;  // 1: the loss covers the K' information bits only
   int64_t nw = 0;        // weights per kind (scales, offsets)
   float* d_w = nullptr;  // [2 nw]: scales then offsets
@@ -743,9 +750,36 @@ cb_status nms_buffers(cb_nms* h, int64_t n, bool train) {
 // no room left beside the posteriors; with small Z a dozen CTAs at different iterations
 // thrash that cache, and each iteration's weights are staged in shared memory instead.
 // Then `w` receives a host copy of the weights (scales then offsets).
+// The graph-specialised learned kernel serves evaluation when the code's plain decoder is
+// the graph-specialised one, the weights are shared and fit the launch parameters, and
+// the lifting is large: the same results as the table-driven learned decoder, at 1.44x
+// the plain decoder's time per iteration on BG1 Z = 384 (C5 at its FER 1e-3 point: 9.2 ms
+// for 8192 frames, 13.8 ms with the table-driven kernel).  With Z = 52 (C4) a dozen CTAs
+// share an SM, and with its weights read from the launch parameters it ran 2.5-3.4x the
+// plain decoder's time per iteration, slower than the table-driven kernel with its weights
+// in shared memory, which such codes keep.
+int nms_nr_grid(cb_nms* h) {
+  cb_code* c = h->code;
+  if (h->nr_grid >= 0) return h->nr_grid;
+  h->nr_grid = 0;
+  // the weight rows of T iterations and the first iteration's zero row
+  if (!c->use_nr || !h->shared || c->dev.z < 128 || h->nw + c->dev.n_entries > cbn::kNrMaxLearnedWeights) return 0;
+  h->nr = cbk::nr_kernel(c->host, c->device, c->nr.specialized, nullptr, true);
+  int g = h->nr.fn ? cbk::nr_learned_grid_size(h->nr, c->host, c->device) : 0;
+  if (g <= 0 && h->nr.specialized) {
+    cudaGetLastError();
+    h->nr = cbk::nr_kernel(c->host, c->device, false, nullptr, true);
+    g = h->nr.fn ? cbk::nr_learned_grid_size(h->nr, c->host, c->device) : 0;
+  }
+  cudaGetLastError();
+  // the code's state slots were allocated for the plain decoder's grid
+  h->nr_grid = std::max(0, std::min(g, c->decode_grid));
+  return h->nr_grid;
+}
+
 cb_status nms_param_weights(cb_nms* h, std::vector<float>& w, bool& in_params) {
   cb_code* c = h->code;
-  in_params = h->shared && h->nw <= cbk::kMaxParamWeights && c->dev.z >= 128;
+  in_params = nms_nr_grid(h) > 0 || (h->shared && h->nw <= cbk::kMaxParamWeights && c->dev.z >= 128);
   if (!in_params) return CB_OK;
   w.resize((size_t)2 * h->nw);
   CB_CUDA(c, cudaMemcpyAsync(w.data(), h->d_w, w.size() * 4, cudaMemcpyDeviceToHost, c->stream));
@@ -779,6 +813,31 @@ cb_status nms_eval(cb_nms* h, const float* llr, int64_t n, const uint32_t* ref, 
   // shared weights not in the launch parameters: each iteration's staged in shared memory
   a.l_smem = h->shared && !param_w;
   CB_CUDA(c, cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), s));
+  if (param_w && h->nr_grid > 0) {
+    // ~30 KB of launch parameters: built once per call site, copied by the launch
+    static thread_local cbn::NrLearnedArgs la;
+    la.a = c->nr_args;
+    la.a.max_iterations = h->T;
+    la.a.llr = llr;
+    la.a.n_frames = n;
+    la.a.bits_out = nullptr;
+    la.a.app_out = nullptr;
+    la.a.iters_out = iters;
+    la.a.ref_bits = ref;
+    la.a.results = reinterpret_cast<cbn::FrameRecord*>(results);
+    la.a.state = reinterpret_cast<unsigned char*>(c->d_state);
+    la.a.work_counter = c->d_counter;
+    la.post_out = post;
+    // row 0: scale 0, offset +inf (no old messages in the first iteration); then the
+    // network's rows
+    const int ne = c->dev.n_entries;
+    std::fill(la.alpha, la.alpha + ne, 0.0f);
+    std::fill(la.beta, la.beta + ne, std::numeric_limits<float>::infinity());
+    std::memcpy(la.alpha + ne, param_w->data(), (size_t)h->nw * 4);
+    std::memcpy(la.beta + ne, param_w->data() + h->nw, (size_t)h->nw * 4);
+    CB_CUDA(c, cbk::nr_learned_launch(h->nr, la, (int)std::min<int64_t>(h->nr_grid, n), s));
+    return CB_OK;
+  }
   const int grid = (int)std::min<int64_t>(c->decode_grid, n);
   if (param_w) {
     // ~30 KB of launch parameters: built once per call site, copied by the launch

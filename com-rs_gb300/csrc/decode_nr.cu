@@ -37,7 +37,10 @@ extern char** environ;  // passed to the compiler process
 namespace cbk {
 namespace {
 
-const void* generic_kernel(int bg) {
+const void* generic_kernel(int bg, bool learned) {
+  if (learned)
+    return bg == 1 ? (const void*)&cbn::layered_nr_kernel<1, cbn::RuntimeLifting, cbn::NrLearnedArgs>
+                   : (const void*)&cbn::layered_nr_kernel<2, cbn::RuntimeLifting, cbn::NrLearnedArgs>;
   return bg == 1 ? (const void*)&cbn::layered_nr_kernel<1, cbn::RuntimeLifting>
                  : (const void*)&cbn::layered_nr_kernel<2, cbn::RuntimeLifting>;
 }
@@ -134,15 +137,18 @@ const std::string& nvcc_path() {
   return path;
 }
 
-// the code's own kernel: Z and the shifts (row-major) as constants
-std::string jit_source(const cbh::NrCode& h) {
+// the code's own kernel: Z and the shifts (row-major) as constants; the plain decoder or
+// the learned min-sum
+std::string jit_source(const cbh::NrCode& h, bool learned) {
   std::ostringstream s;
   s << "#include \"layered_nr.cuh\"\nnamespace cbn {\nstruct FixedLifting {\n"
     << "  static constexpr bool fixed = true;\n  static constexpr int z = " << h.z << ";\n"
     << "  static constexpr int shift[" << h.entry_shift.size() << "] = {";
   for (size_t t = 0; t < h.entry_shift.size(); t++) s << (t ? ", " : "") << h.entry_shift[t];
-  s << "};\n};\n}  // namespace cbn\n"
-    << "template __global__ void cbn::layered_nr_kernel<" << h.bg << ", cbn::FixedLifting>(const __grid_constant__ cbn::NrArgs);\n";
+  s << "};\n};\n}  // namespace cbn\n";
+  const char* P = learned ? "cbn::NrLearnedArgs" : "cbn::NrArgs";
+  s << "template __global__ void cbn::layered_nr_kernel<" << h.bg << ", cbn::FixedLifting, " << P
+    << ">(const __grid_constant__ " << P << ");\n";
   return s.str();
 }
 
@@ -313,6 +319,9 @@ std::map<std::pair<cudaKernel_t, int>, size_t> g_jit_smem_set;  // (kernel, devi
 
 }  // namespace
 
+// the learned kernel's launch parameters stay within the 32,764 bytes a launch takes
+static_assert(sizeof(cbn::NrLearnedArgs) <= 32764, "NrLearnedArgs exceeds the launch parameter limit");
+
 void fill_nr_args(const cbh::NrCode& h, cbn::NrArgs& a) {
   std::memset(&a, 0, sizeof a);
   a.z = h.z;
@@ -335,12 +344,12 @@ size_t nr_smem(const cbh::NrCode& h) {
   return cbn::nr_smem_bytes(h.n_full, h.z, h.rows_n, (int)h.entry_col.size());
 }
 
-bool nr_prepare(const cbh::NrCode& h, std::string* note) {
+bool nr_prepare(const cbh::NrCode& h, std::string* note, bool learned) {
   if (!matches_base_graph(h)) {
     if (note) *note = "entries not in the base graph's order";
     return false;
   }
-  const std::string src = jit_source(h);
+  const std::string src = jit_source(h, learned);
   const std::string key = cache_key(h, src), dir = cache_dir();
   std::vector<char> cubin;
   if (!dir.empty() && read_file(dir + "/" + key, cubin)) return true;
@@ -349,16 +358,16 @@ bool nr_prepare(const cbh::NrCode& h, std::string* note) {
   return true;
 }
 
-NrKernel nr_kernel(const cbh::NrCode& h, int device, bool specialize, std::string* note) {
+NrKernel nr_kernel(const cbh::NrCode& h, int device, bool specialize, std::string* note, bool learned) {
   NrKernel k;
-  k.fn = generic_kernel(h.bg);
+  k.fn = generic_kernel(h.bg, learned);
   if (!matches_base_graph(h)) {
     k.fn = nullptr;
     if (note) *note = "entries not in the base graph's order";
     return k;
   }
   if (!specialize) return k;
-  const std::string src = jit_source(h);
+  const std::string src = jit_source(h, learned);
   const std::string key = cache_key(h, src);
   std::lock_guard<std::mutex> lock(g_jit_mu);
   auto it = g_jit_kernels.find(key);
@@ -422,6 +431,27 @@ cudaError_t nr_launch(const NrKernel& k, const cbn::NrArgs& a, int grid, cudaStr
   cudaError_t e = set_smem(k, smem, device);
   if (e != cudaSuccess) return e;
   void* args[] = {(void*)&a};
+  return cudaLaunchKernel(k.fn, dim3(grid), dim3(((a.z + 31) / 32) * 32), args, smem, stream);
+}
+
+int nr_learned_grid_size(const NrKernel& k, const cbh::NrCode& h, int device) {
+  const size_t smem = cbn::nr_learned_smem_bytes(h.n_full, h.z, h.rows_n, (int)h.entry_col.size());
+  if (set_smem(k, smem, device) != cudaSuccess) return 0;
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, ((h.z + 31) / 32) * 32, smem) != cudaSuccess)
+    return 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  return per_sm * sms;
+}
+
+cudaError_t nr_learned_launch(const NrKernel& k, const cbn::NrLearnedArgs& la, int grid, cudaStream_t stream) {
+  const cbn::NrArgs& a = la.a;
+  const size_t smem = cbn::nr_learned_smem_bytes(a.n_full, a.z, a.rows, a.n_entries);
+  int device = 0;
+  cudaGetDevice(&device);
+  cudaError_t e = set_smem(k, smem, device);
+  if (e != cudaSuccess) return e;
+  void* args[] = {(void*)&la};
   return cudaLaunchKernel(k.fn, dim3(grid), dim3(((a.z + 31) / 32) * 32), args, smem, stream);
 }
 

@@ -84,6 +84,67 @@ __host__ __device__ inline size_t nr_smem_bytes(int n_full, int z, int rows, int
   return (b + 15) & ~(size_t)15;
 }
 
+// The learned min-sum (shared weights per base-graph entry and iteration): the plain
+// decoder's arguments, an optional full-posterior output, and the weights in the launch
+// parameters (read through the constant cache: every thread of a CTA reads the same one).
+constexpr int kNrMaxLearnedWeights = 3200;  // per kind: (iterations + 1) x entries
+struct NrLearnedArgs {
+  NrArgs a;
+  float* post_out;  // [n_frames][n_full] a posteriori LLRs of the whole word (optional)
+  float alpha[kNrMaxLearnedWeights];  // [1 + iteration][entry] scales (row 0: 0)
+  float beta[kNrMaxLearnedWeights];   // [1 + iteration][entry] offsets (row 0: +inf)
+};
+
+// Weights of one iteration for the rows: none (the plain decoder's rule), or the
+// learned scales and offsets of this iteration (cur) and of the previous one (prev, for
+// the old messages), indexed by entry, as (scale, offset) pairs in shared memory.
+struct NrNoWeights {
+  static constexpr bool learned = false;
+};
+struct NrRowWeights {
+  static constexpr bool learned = true;
+  const float2 *prev, *cur;
+  __device__ __forceinline__ float ap(int i) const { return prev[i].x; }
+  __device__ __forceinline__ float bp(int i) const { return prev[i].y; }
+  __device__ __forceinline__ float ac(int i) const { return cur[i].x; }
+  __device__ __forceinline__ float bc(int i) const { return cur[i].y; }
+};
+struct NrNoWeightSet {
+  static constexpr bool learned = false;
+  __device__ __forceinline__ NrNoWeights at(int) const { return {}; }
+};
+// The weight rows [T + 1][entries] of the launch parameters: row t + 1 holds iteration
+// t's, row 0 the scale 0 and the offset +inf, whose magnitude max(0 m - inf, 0) is 0 for
+// every old message of the first iteration (which has none): no branch on the first
+// iteration in the rows.  Each iteration's row is staged in shared memory, in the buffer
+// the iteration before last used (two buffers of `ne` pairs): the rows then read them
+// with one 8-byte shared load per edge and message (10.2 against 11.6 ms for 8192 C2
+// codewords and 10 iterations reading the launch parameters through a pointer, 10.3 from
+// a constant array).
+struct NrParamWeightSet {
+  static constexpr bool learned = true;
+  float2* buf;  // shared memory: 2 x ne pairs
+  const float* alpha;
+  const float* beta;
+  int ne;  // entries
+  __device__ __forceinline__ NrRowWeights at(int t) const {
+    float2* cur = buf + ((t + 1) & 1) * ne;
+    for (int i = threadIdx.x; i < ne; i += blockDim.x)
+      cur[i] = make_float2(alpha[(t + 1) * ne + i], beta[(t + 1) * ne + i]);
+    if (t == 0) {
+      float2* first = buf + (t & 1) * ne;
+      for (int i = threadIdx.x; i < ne; i += blockDim.x) first[i] = make_float2(alpha[i], beta[i]);
+    }
+    __syncthreads();
+    return {buf + (t & 1) * ne, cur};
+  }
+};
+
+// shared memory of the learned kernel: the plain decoder's and the two weight buffers
+__host__ __device__ inline size_t nr_learned_smem_bytes(int n_full, int z, int rows, int n_entries) {
+  return nr_smem_bytes(n_full, z, rows, n_entries) + (size_t)n_entries * 2 * sizeof(float2);
+}
+
 // Z and the shifts from the launch parameters
 struct RuntimeLifting {
   static constexpr bool fixed = false;
@@ -201,6 +262,70 @@ __device__ __forceinline__ void nr_row(unsigned char* post, const NrArgs& a, int
   nm = (sm << 8) | i1;
 }
 
+// The learned message magnitude max(alpha m - beta, 0), rounded as the training forward
+// (nms_learned.cu) and LearnedRowW (decode_common.cuh) compute it.  fmaxf agrees with
+// their `am > 0 ? am : 0` except perhaps on the sign of a zero from am = -0; a message of
+// magnitude zero adds or subtracts zero whatever its sign, so the posteriors are the
+// same bits (the sign bit kept for it only ever multiplies that zero again).
+__device__ __forceinline__ float learned_mag(float al, float be, float m) {
+  return fmaxf(__fsub_rn(__fmul_rn(al, m), be), 0.f);
+}
+
+// One lifted row of the learned min-sum (row_update_learned of decode_common.cuh, with
+// the addresses from edge_offset and the weights of entry S0 + i): the state keeps the
+// raw minimum and second minimum, each edge's message magnitude is max(alpha m - beta, 0)
+// with its own weights, the previous iteration's for the old message (in the first
+// iteration the state is zero and the weight row gives 0: x = p - 0, as the training
+// forward's first iteration).
+template <int BG, class K, int S0, int D, class RW>
+__device__ __forceinline__ void nr_row_learned(unsigned char* post, const NrArgs& a, int r, int r4, int z4,
+                                               const RW& w, float a1, float a2, uint32_t mt, float& n1, float& n2,
+                                               uint32_t& nm) {
+  int off[D];
+  float x[D];
+  const int old_i1 = (int)(mt & 31u);
+  const uint32_t t0 = mt << (24 - D);
+  row_offsets<BG, K, S0, 0, D>(off, a, r, r4, z4);
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    const float mag = learned_mag(w.ap(S0 + i), w.bp(S0 + i), (i == old_i1) ? a2 : a1);
+    const uint32_t neg = (__float_as_uint(mag) ^ 0x80000000u) ^ ((t0 << i) & 0x80000000u);
+    x[i] = __fadd_rn(ld_f(post, off[i]), __uint_as_float(neg));
+  }
+  float m1 = __int_as_float(0x7f800000), m2 = __int_as_float(0x7f800000);
+#pragma unroll
+  for (int i = 0; i + 1 < D; i += 2) {
+    const float s = min_xorsign_abs(x[i], x[i + 1]);
+    const float l = fmaxf(fabsf(x[i]), fabsf(x[i + 1]));
+    m2 = min3f(m2, fmaxf(fabsf(m1), fabsf(s)), l);
+    m1 = min_xorsign_abs(m1, s);
+  }
+  if (D & 1) {
+    m2 = fminf(m2, fmaxf(fabsf(m1), fabsf(x[D - 1])));
+    m1 = min_xorsign_abs(m1, x[D - 1]);
+  }
+  const uint32_t ps = __float_as_uint(m1) & 0x80000000u;
+  m1 = fabsf(m1);
+  // the raw magnitude m2 where |x| equals the minimum, else m1, and the index sum, by the
+  // multiply-adds of nr_row
+  const uint32_t dneg = __float_as_uint(m1) - __float_as_uint(m2);
+  uint32_t sm = 0, i1 = 0;
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    uint32_t eqm, mb;
+    asm("set.eq.u32.f32 %0, %1, %2;" : "=r"(eqm) : "f"(fabsf(x[i])), "f"(m1));
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(mb) : "r"(eqm), "r"(dneg), "r"(__float_as_uint(m1)));
+    if (i) asm("mad.lo.u32 %0, %1, %2, %0;" : "+r"(i1) : "r"(eqm), "r"((uint32_t)-i));
+    const float mag = learned_mag(w.ac(S0 + i), w.bc(S0 + i), __uint_as_float(mb));
+    const uint32_t ob = __float_as_uint(mag) | ((ps ^ __float_as_uint(x[i])) & 0x80000000u);
+    st_f(post, off[i], __fadd_rn(x[i], __uint_as_float(ob)));
+    sm = (sm << 1) | (ob >> 31);
+  }
+  n1 = m1;
+  n2 = m2;
+  nm = (sm << 8) | i1;
+}
+
 struct NrState {
   unsigned char* mag;
   unsigned char* meta;
@@ -228,10 +353,11 @@ struct NrState {
 // NrTuning::ahead = 2 the state of row Q arrives as a*, that of row Q + 1 as b*, and row
 // Q + 2's is loaded here (c*), so that the L2 latency of the loads is not the first wait
 // of every row; with ahead = 0 each row loads its own state.
-template <int BG, class K, int Q>
+template <int BG, class K, int Q, class W>
 __device__ __forceinline__ void nr_iteration(unsigned char* post, const NrArgs& a, const NrState& st, int r, int r4,
-                                             int z4, int z, bool active, bool first, bool nms, float alpha, float a1,
-                                             float a2, uint32_t mt, float b1, float b2, uint32_t bt) {
+                                             int z4, int z, bool active, bool first, bool nms, float alpha,
+                                             const W& w, float a1, float a2, uint32_t mt, float b1, float b2,
+                                             uint32_t bt) {
   if constexpr (Q < Graph<BG>::rows) {
     constexpr int L = Graph<BG>::order[Q];
     constexpr int S0 = Graph<BG>::start[L];
@@ -254,11 +380,14 @@ __device__ __forceinline__ void nr_iteration(unsigned char* post, const NrArgs& 
       }
       float n1, n2;
       uint32_t nm;
-      nr_row<BG, K, S0, D>(post, a, rr, rr4, z4, a1, a2, mt, nms, alpha, n1, n2, nm);
+      if constexpr (W::learned)
+        nr_row_learned<BG, K, S0, D>(post, a, rr, rr4, z4, w, a1, a2, mt, n1, n2, nm);
+      else
+        nr_row<BG, K, S0, D>(post, a, rr, rr4, z4, a1, a2, mt, nms, alpha, n1, n2, nm);
       st.store(L * zz + rr, n1, n2, nm);
     }
     if constexpr (Graph<BG>::level_end[Q] != 0) __syncthreads();
-    nr_iteration<BG, K, Q + 1>(post, a, st, r, r4, z4, z, active, first, nms, alpha, b1, b2, bt, c1, c2, ct);
+    nr_iteration<BG, K, Q + 1>(post, a, st, r, r4, z4, z, active, first, nms, alpha, w, b1, b2, bt, c1, c2, ct);
   }
 }
 
@@ -293,10 +422,30 @@ __device__ __forceinline__ bool some_nr_check_fails(const float* post, uint32_t*
   return some_packed_check_fails(post, hd, ent, lstart, a.rows, ncol, z, tid, nt);
 }
 
-// Persistent kernel: each CTA takes codewords from the work counter, one thread per
+// The decoder arguments, the learned weights (none for the plain rule) and the whole
+// word's a posteriori output of a launch's parameters.
+__device__ __forceinline__ const NrArgs& nr_args_of(const NrArgs& p) { return p; }
+__device__ __forceinline__ const NrArgs& nr_args_of(const NrLearnedArgs& p) { return p.a; }
+__device__ __forceinline__ NrNoWeightSet nr_weights_of(const NrArgs&) { return {}; }
+__device__ __forceinline__ NrParamWeightSet nr_weights_of(const NrLearnedArgs& p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const NrArgs& a = p.a;
+  float2* buf = reinterpret_cast<float2*>(smem + nr_smem_bytes(a.n_full, a.z, a.rows, a.n_entries));
+  return {buf, p.alpha, p.beta, a.n_entries};
+}
+__device__ __forceinline__ float* nr_post_out_of(const NrArgs&) { return nullptr; }
+__device__ __forceinline__ float* nr_post_out_of(const NrLearnedArgs& p) { return p.post_out; }
+
+// Persistent decoder: each CTA takes codewords from the work counter, one thread per
 // lifted row, posteriors in shared memory, check-node state in its own L2-resident slot.
-template <int BG, class K>
-__global__ void __launch_bounds__(384, 2) layered_nr_kernel(const __grid_constant__ NrArgs a) {
+// P = NrArgs: the plain rule; P = NrLearnedArgs: the learned min-sum with shared weights
+// (its a.max_iterations is the network's T).  The body stays in the kernel: as a device
+// function taking the parameters by reference the plain decoder ran 9 % slower.
+template <int BG, class K, class P = NrArgs>
+__global__ void __launch_bounds__(384, 2) layered_nr_kernel(const __grid_constant__ P p) {
+  const NrArgs& a = nr_args_of(p);
+  const auto wset = nr_weights_of(p);
+  float* const post_out = nr_post_out_of(p);
   extern __shared__ __align__(16) unsigned char smem[];
   const int z = K::fixed ? K::z : a.z;
   const int nt = blockDim.x, tid = threadIdx.x;
@@ -379,7 +528,7 @@ __global__ void __launch_bounds__(384, 2) layered_nr_kernel(const __grid_constan
           }
         }
         nr_iteration<BG, K, 0>(reinterpret_cast<unsigned char*>(post), a, st, tid, r4, z4, z, active, iter == 1, nms,
-                               alpha, a1, a2, mt, b1, b2, bt);
+                               alpha, wset.at(iter - 1), a1, a2, mt, b1, b2, bt);
         if (!some_nr_check_fails<BG, K>(post, hd, s_ent, s_lstart, a, ncol, z, tid, nt, r4, z4)) {
           it = iter;
           break;
@@ -417,6 +566,8 @@ __global__ void __launch_bounds__(384, 2) layered_nr_kernel(const __grid_constan
     }
     if (a.app_out)
       for (int v = tid; v < a.k_info; v += nt) a.app_out[(size_t)cw * a.k_info + v] = post[v];
+    if (post_out)
+      for (int v = tid; v < n_full; v += nt) post_out[(size_t)cw * n_full + v] = post[v];
     if (be) atomicAdd(&s_err, be);
     __syncthreads();
     if (tid == 0) {

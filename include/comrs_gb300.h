@@ -88,9 +88,10 @@ const char* cb_last_error(const cb_code* code);
  * log where the reference calls the platform libm. */
 cb_status cb_code_set_demapper(cb_code* code, int32_t exact);
 
-/* Compile, without a GPU, the decoder of an f32 layered min-sum code for its base graph
- * and lifting size (Z and every shift as constants) and store it in the on-disk cache
- * that the code's first device call reads (for build steps that warm the cache).
+/* Compile, without a GPU, the decoders of an f32 layered min-sum code for its base graph
+ * and lifting size (Z and every shift as constants: the plain rule's and the learned
+ * min-sum's evaluation) and store them in the on-disk cache that the code's first device
+ * call reads (for build steps that warm the cache).
  * CB_ERR_CONFIG for other codes, CB_ERR_IO when no compiler is found or it fails. */
 cb_status cb_code_prepare(cb_code* code);
 
