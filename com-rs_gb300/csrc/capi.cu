@@ -396,7 +396,7 @@ cb_status ensure_device(cb_code* c) {
   // the run-time compiler is at hand, else the base graph's build
   if (c->precision == CB_F32 && !c->generic && c->cfg.layered &&
       (c->cfg.rule == cbd::RULE_NMS || c->cfg.rule == cbd::RULE_OMS)) {
-    c->nr = cbk::nr_kernel(h, c->device, true, &c->nr_note);
+    c->nr = cbk::nr_kernel(h, c->device, true, &c->nr_note, false, c->cfg.rule);
     int g = c->nr.fn ? cbk::nr_grid_size(c->nr, h, c->device) : 0;
     if (g <= 0 && c->nr.specialized) {
       cudaGetLastError();
@@ -525,7 +525,8 @@ cb_status cb_code_prepare(cb_code* c) {
     return fail(c, CB_ERR_CONFIG, "only f32 layered min-sum codes run a decoder compiled for their lifting");
   std::lock_guard<std::mutex> lock(c->mu);
   std::string note;
-  if (!cbk::nr_prepare(c->host, &note)) return fail(c, CB_ERR_IO, "no decoder compiled for this lifting: " + note);
+  if (!cbk::nr_prepare(c->host, &note, false, c->cfg.rule))
+    return fail(c, CB_ERR_IO, "no decoder compiled for this lifting: " + note);
   if (!cbk::nr_prepare(c->host, &note, true))
     return fail(c, CB_ERR_IO, "no learned decoder compiled for this lifting: " + note);
   return CB_OK;
@@ -700,6 +701,10 @@ struct cb_nms {
   int info_only_loss = 0;  // 1: the loss covers the K' information bits only
   int64_t nw = 0;        // weights per kind (scales, offsets)
   float* d_w = nullptr;  // [2 nw]: scales then offsets
+  // a host copy of d_w for the launch parameters of evaluation, valid until the weights
+  // change (cb_nms_set_weights, a training step)
+  std::vector<float> h_w;
+  bool h_w_valid = false;
   float* d_g = nullptr;
   float* d_m = nullptr;
   float* d_v = nullptr;
@@ -781,9 +786,13 @@ cb_status nms_param_weights(cb_nms* h, std::vector<float>& w, bool& in_params) {
   cb_code* c = h->code;
   in_params = nms_nr_grid(h) > 0 || (h->shared && h->nw <= cbk::kMaxParamWeights && c->dev.z >= 128);
   if (!in_params) return CB_OK;
-  w.resize((size_t)2 * h->nw);
-  CB_CUDA(c, cudaMemcpyAsync(w.data(), h->d_w, w.size() * 4, cudaMemcpyDeviceToHost, c->stream));
-  CB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (!h->h_w_valid) {
+    h->h_w.resize((size_t)2 * h->nw);
+    CB_CUDA(c, cudaMemcpyAsync(h->h_w.data(), h->d_w, h->h_w.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+    CB_CUDA(c, cudaStreamSynchronize(c->stream));
+    h->h_w_valid = true;
+  }
+  w = h->h_w;
   return CB_OK;
 }
 
@@ -957,6 +966,7 @@ cb_status cb_nms_set_weights(cb_nms* h, const float* alpha, const float* beta) {
   cb_code* c = h->code;
   std::lock_guard<std::mutex> lock(c->mu);
   CB_CUDA(c, cudaSetDevice(c->device));
+  h->h_w_valid = false;
   CB_CUDA(c, cudaMemcpy(h->d_w, alpha, sizeof(float) * h->nw, cudaMemcpyHostToDevice));
   CB_CUDA(c, cudaMemcpy(h->d_w + h->nw, beta, sizeof(float) * h->nw, cudaMemcpyHostToDevice));
   CB_CUDA(c, cudaMemset(h->d_m, 0, sizeof(float) * 2 * h->nw));
@@ -1034,6 +1044,7 @@ cb_status cb_nms_train_step(cb_nms* h, int32_t m, uint64_t seed, uint64_t name_h
     return s2;
   if (cb_status s3 = nms_fwd_bwd(h, batch, true, multi_loss, c->stream)) return s3;
   h->step++;
+  h->h_w_valid = false;
   CB_CUDA(c, cbk::launch_adam(h->d_w, h->d_g, h->d_m, h->d_v, 2 * h->nw, (float)lr, h->step, c->stream));
   float l = 0.f;
   CB_CUDA(c, cudaMemcpyAsync(&l, h->d_loss, 4, cudaMemcpyDeviceToHost, c->stream));

@@ -54,6 +54,37 @@ __host__ __device__ __forceinline__ size_t decode_smem_bytes(int n_full, int z, 
 // in the launch parameters, or each iteration's staged in shared memory
 enum LearnedWeights { kPlain = 0, kWeightsGlobal = 1, kWeightsParam = 2, kWeightsShared = 3 };
 
+// One layered iteration of decode_body: the rows in schedule order, each row's state from
+// the previous iteration (L2-resident: loaded where it is used), a barrier after each level.
+template <typename T, int LW, int RULE>
+__device__ __forceinline__ void decode_layers(const cbd::DevCode& c, T* post, const StateSlot<T>& st,
+                                              const LearnedRowW& lw, int iter, int tid, int z, bool active,
+                                              T alpha) {
+  for (int q = 0; q < c.rows_n; q++) {
+    const int L = c.layer_order[q];
+    T a1 = (T)0, a2 = (T)0;
+    uint32_t mt = 0;
+    if (iter > 1 && active) st.load(L * z + tid, a1, a2, mt);
+    if (active) {
+      const int s0 = c.layer_start[L];
+      const int d = c.layer_start[L + 1] - s0;
+      T n1, n2;
+      uint32_t nm;
+      if constexpr (LW != kPlain)
+        row_dispatch_learned(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z},
+                             LearnedRowW{lw.a_prev, lw.b_prev, lw.a_cur, lw.b_cur, s0, lw.stride, lw.roff}, iter - 1,
+                             iter == 1, a1, a2, mt, n1, n2, nm);
+      else if constexpr (sizeof(T) == 4)
+        row_dispatch_lean<RULE>(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z}, a1, a2, mt, alpha, n1, n2,
+                                nm);
+      else
+        row_dispatch<T, RULE>(d, post, c.entry + s0, tid, z, a1, a2, mt, alpha, n1, n2, nm);
+      st.store(L * z + tid, n1, n2, nm);
+    }
+    if (c.level_end[q]) __syncthreads();
+  }
+}
+
 template <typename T, int LW>
 __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float* la, const float* lb) {
   constexpr bool LEARNED = LW != kPlain;
@@ -156,30 +187,13 @@ __device__ __forceinline__ void decode_body(const DecodeArgs<T>& a, const float*
             }
           }
         }
-        // the row's state from the previous iteration (L2-resident: loaded where it is used)
-        for (int q = 0; q < c.rows_n; q++) {
-          const int L = c.layer_order[q];
-          T a1 = (T)0, a2 = (T)0;
-          uint32_t mt = 0;
-          if (iter > 1 && active) st.load(L * z + tid, a1, a2, mt);
-          if (active) {
-            const int s0 = c.layer_start[L];
-            const int d = c.layer_start[L + 1] - s0;
-            T n1, n2;
-            uint32_t nm;
-            if constexpr (LEARNED)
-              row_dispatch_learned(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z},
-                                   LearnedRowW{w_ap, w_bp, w_ac, w_bc, s0, w_stride, w_roff}, iter - 1,
-                                   iter == 1, a1, a2, mt, n1, n2, nm);
-            else if constexpr (sizeof(T) == 4)
-              row_dispatch_lean(d, post, EdgeAddrTable{c.eaddr + s0, tid, 4 * tid, 4 * z}, a1, a2, mt, rule, alpha,
-                                n1, n2, nm);
-            else
-              row_dispatch<T>(d, post, c.entry + s0, tid, z, a1, a2, mt, rule, alpha, n1, n2, nm);
-            st.store(L * z + tid, n1, n2, nm);
-          }
-          if (c.level_end[q]) __syncthreads();
-        }
+        // the rows of one iteration, the rule a template parameter (one branch around the
+        // whole iteration, none in the rows)
+        const LearnedRowW lw{w_ap, w_bp, w_ac, w_bc, 0, w_stride, w_roff};
+        if (LEARNED || rule == cbd::RULE_NMS)
+          decode_layers<T, LW, cbd::RULE_NMS>(c, post, st, lw, iter, tid, z, active, alpha);
+        else
+          decode_layers<T, LW, cbd::RULE_OMS>(c, post, st, lw, iter, tid, z, active, alpha);
         if (!some_check_fails(post, hd, s_ent, s_lstart, c.rows_n, ncol, z, tid, nt)) {
           it = iter;
           break;

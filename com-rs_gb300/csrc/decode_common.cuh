@@ -13,10 +13,13 @@ namespace {
 
 // One lifted row of a layer: thread r, degree D known at compile time.
 // old state (a1, a2, mt) -> new state (n1, n2, nm); post updated in place.
-template <typename T, int D>
+// RULE (cbd::RULE_NMS or RULE_OMS) is a template parameter: with the rule read at run time
+// the compiler computed both rules' magnitudes in every row and kept one (C2 in f64:
+// 42.4 against 36.9 ms per 2048 codewords, 3.9 against 3.3 FP64 instructions per edge
+// update).
+template <typename T, int D, int RULE>
 __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t* __restrict__ ent, int r, int z,
-                                           T a1, T a2, uint32_t mt, int rule, T alpha, T& n1, T& n2,
-                                           uint32_t& nm) {
+                                           T a1, T a2, uint32_t mt, T alpha, T& n1, T& n2, uint32_t& nm) {
   int off[D];
   T x[D];
   const int old_i1 = (int)(mt & 31u);
@@ -77,7 +80,7 @@ __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t*
       i1 = lt ? e : i1;
     }
   }
-  if (rule == cbd::RULE_NMS) {
+  if constexpr (RULE == cbd::RULE_NMS) {
     n1 = mul_rn(alpha, m1);
     n2 = mul_rn(alpha, m2);
   } else {
@@ -131,10 +134,9 @@ struct EdgeAddrTable {
 //   * outgoing signs are applied and collected with bit operations.
 // State word: bits 0-4 an edge holding the second minimum, bits 8.. the outgoing sign of
 // edge e at bit 8 + (D - 1 - e).
-template <int D, typename Addr>
+template <int D, int RULE, typename Addr>
 __device__ __forceinline__ void row_update_lean(float* __restrict__ post, const Addr& addr, float a1, float a2,
-                                                uint32_t mt, int rule, float alpha, float& n1, float& n2,
-                                                uint32_t& nm) {
+                                                uint32_t mt, float alpha, float& n1, float& n2, uint32_t& nm) {
   int off[D];
   float x[D];
   const int old_i1 = (int)(mt & 31u);
@@ -162,7 +164,7 @@ __device__ __forceinline__ void row_update_lean(float* __restrict__ post, const 
   }
   const uint32_t ps = __float_as_uint(m1) & 0x80000000u;
   m1 = fabsf(m1);
-  if (rule == cbd::RULE_NMS) {
+  if constexpr (RULE == cbd::RULE_NMS) {
     n1 = __fmul_rn(alpha, m1);
     n2 = __fmul_rn(alpha, m2);
   } else {
@@ -272,37 +274,36 @@ __device__ __forceinline__ void row_dispatch_learned(int d, float* post, const A
   }
 }
 
-template <typename Addr>
+template <int RULE, typename Addr>
 __device__ __forceinline__ void row_dispatch_lean(int d, float* post, const Addr& addr, float a1, float a2,
-                                                  uint32_t mt, int rule, float alpha, float& n1, float& n2,
-                                                  uint32_t& nm) {
+                                                  uint32_t mt, float alpha, float& n1, float& n2, uint32_t& nm) {
   switch (d) {
-    case 3: row_update_lean<3>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 4: row_update_lean<4>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 5: row_update_lean<5>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 6: row_update_lean<6>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 7: row_update_lean<7>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 8: row_update_lean<8>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 9: row_update_lean<9>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 10: row_update_lean<10>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    default: row_update_lean<19>(post, addr, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 3: row_update_lean<3, RULE>(post, addr, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 4: row_update_lean<4, RULE>(post, addr, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 5: row_update_lean<5, RULE>(post, addr, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 6: row_update_lean<6, RULE>(post, addr, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 7: row_update_lean<7, RULE>(post, addr, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 8: row_update_lean<8, RULE>(post, addr, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 9: row_update_lean<9, RULE>(post, addr, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 10: row_update_lean<10, RULE>(post, addr, a1, a2, mt, alpha, n1, n2, nm); break;
+    default: row_update_lean<19, RULE>(post, addr, a1, a2, mt, alpha, n1, n2, nm); break;
   }
 }
 
 // the row update of the f64 decoder (f32 rows take row_dispatch_lean)
-template <typename T>
+template <typename T, int RULE>
 __device__ __forceinline__ void row_dispatch(int d, T* post, const uint32_t* ent, int r, int z, T a1, T a2,
-                                             uint32_t mt, int rule, T alpha, T& n1, T& n2, uint32_t& nm) {
+                                             uint32_t mt, T alpha, T& n1, T& n2, uint32_t& nm) {
   switch (d) {
-    case 3: row_update<T, 3>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 4: row_update<T, 4>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 5: row_update<T, 5>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 6: row_update<T, 6>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 7: row_update<T, 7>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 8: row_update<T, 8>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 9: row_update<T, 9>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    case 10: row_update<T, 10>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
-    default: row_update<T, 19>(post, ent, r, z, a1, a2, mt, rule, alpha, n1, n2, nm); break;
+    case 3: row_update<T, 3, RULE>(post, ent, r, z, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 4: row_update<T, 4, RULE>(post, ent, r, z, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 5: row_update<T, 5, RULE>(post, ent, r, z, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 6: row_update<T, 6, RULE>(post, ent, r, z, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 7: row_update<T, 7, RULE>(post, ent, r, z, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 8: row_update<T, 8, RULE>(post, ent, r, z, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 9: row_update<T, 9, RULE>(post, ent, r, z, a1, a2, mt, alpha, n1, n2, nm); break;
+    case 10: row_update<T, 10, RULE>(post, ent, r, z, a1, a2, mt, alpha, n1, n2, nm); break;
+    default: row_update<T, 19, RULE>(post, ent, r, z, a1, a2, mt, alpha, n1, n2, nm); break;
   }
 }
 

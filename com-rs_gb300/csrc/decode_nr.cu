@@ -137,15 +137,15 @@ const std::string& nvcc_path() {
   return path;
 }
 
-// the code's own kernel: Z and the shifts (row-major) as constants; the plain decoder or
-// the learned min-sum
-std::string jit_source(const cbh::NrCode& h, bool learned) {
+// the code's own kernel: Z, the shifts (row-major) and the min-sum rule as constants; the
+// plain decoder or the learned min-sum (which has no rule of its own)
+std::string jit_source(const cbh::NrCode& h, bool learned, int rule) {
   std::ostringstream s;
   s << "#include \"layered_nr.cuh\"\nnamespace cbn {\nstruct FixedLifting {\n"
     << "  static constexpr bool fixed = true;\n  static constexpr int z = " << h.z << ";\n"
     << "  static constexpr int shift[" << h.entry_shift.size() << "] = {";
   for (size_t t = 0; t < h.entry_shift.size(); t++) s << (t ? ", " : "") << h.entry_shift[t];
-  s << "};\n};\n}  // namespace cbn\n";
+  s << "};\n  static constexpr int rule = " << (learned ? 1 : rule) << ";\n};\n}  // namespace cbn\n";
   const char* P = learned ? "cbn::NrLearnedArgs" : "cbn::NrArgs";
   s << "template __global__ void cbn::layered_nr_kernel<" << h.bg << ", cbn::FixedLifting, " << P
     << ">(const __grid_constant__ " << P << ");\n";
@@ -344,12 +344,12 @@ size_t nr_smem(const cbh::NrCode& h) {
   return cbn::nr_smem_bytes(h.n_full, h.z, h.rows_n, (int)h.entry_col.size());
 }
 
-bool nr_prepare(const cbh::NrCode& h, std::string* note, bool learned) {
+bool nr_prepare(const cbh::NrCode& h, std::string* note, bool learned, int rule) {
   if (!matches_base_graph(h)) {
     if (note) *note = "entries not in the base graph's order";
     return false;
   }
-  const std::string src = jit_source(h, learned);
+  const std::string src = jit_source(h, learned, rule);
   const std::string key = cache_key(h, src), dir = cache_dir();
   std::vector<char> cubin;
   if (!dir.empty() && read_file(dir + "/" + key, cubin)) return true;
@@ -358,7 +358,7 @@ bool nr_prepare(const cbh::NrCode& h, std::string* note, bool learned) {
   return true;
 }
 
-NrKernel nr_kernel(const cbh::NrCode& h, int device, bool specialize, std::string* note, bool learned) {
+NrKernel nr_kernel(const cbh::NrCode& h, int device, bool specialize, std::string* note, bool learned, int rule) {
   NrKernel k;
   k.fn = generic_kernel(h.bg, learned);
   if (!matches_base_graph(h)) {
@@ -367,7 +367,7 @@ NrKernel nr_kernel(const cbh::NrCode& h, int device, bool specialize, std::strin
     return k;
   }
   if (!specialize) return k;
-  const std::string src = jit_source(h, learned);
+  const std::string src = jit_source(h, learned, rule);
   const std::string key = cache_key(h, src);
   std::lock_guard<std::mutex> lock(g_jit_mu);
   auto it = g_jit_kernels.find(key);

@@ -118,8 +118,12 @@ __device__ void decode_item(const MixDecodeArgs& a, const MixItem& it, unsigned 
             float a1 = 0.f, a2 = 0.f, n1, n2;
             uint32_t mt = 0u, nm;
             if (iter > 1) st.load(L * z + r, a1, a2, mt);
-            row_dispatch_lean(d, post, EdgeAddrTable{s_addr + s0, r, 4 * r, 4 * z}, a1, a2, mt, a.rule, a.alpha, n1,
-                              n2, nm);
+            if (a.rule == cbd::RULE_NMS)
+              row_dispatch_lean<cbd::RULE_NMS>(d, post, EdgeAddrTable{s_addr + s0, r, 4 * r, 4 * z}, a1, a2, mt,
+                                               a.alpha, n1, n2, nm);
+            else
+              row_dispatch_lean<cbd::RULE_OMS>(d, post, EdgeAddrTable{s_addr + s0, r, 4 * r, 4 * z}, a1, a2, mt,
+                                               a.alpha, n1, n2, nm);
             st.store(L * z + r, n1, n2, nm);
           }
         }

@@ -26,8 +26,11 @@ void fill_nr_args(const cbh::NrCode& h, cbn::NrArgs& a);
 // run-time compiler is at hand (built once per base graph and lifting size, then taken
 // from the process's cache or the on-disk cache), else the base graph's kernel.  `note`
 // receives why no specialisation is used, if none is.  `learned`: the learned min-sum's
-// kernel (layered_nr_kernel with NrLearnedArgs) instead of the plain decoder's.
-NrKernel nr_kernel(const cbh::NrCode& h, int device, bool specialize, std::string* note, bool learned = false);
+// kernel (layered_nr_kernel with NrLearnedArgs) instead of the plain decoder's; `rule` the
+// plain decoder's min-sum rule (cbd::RULE_NMS or RULE_OMS), compiled into its
+// specialisation.
+NrKernel nr_kernel(const cbh::NrCode& h, int device, bool specialize, std::string* note, bool learned = false,
+                   int rule = 1);
 
 // resident CTAs of the persistent grid (occupancy x SMs) and the launch
 int nr_grid_size(const NrKernel& k, const cbh::NrCode& h, int device);
@@ -38,6 +41,6 @@ cudaError_t nr_learned_launch(const NrKernel& k, const cbn::NrLearnedArgs& la, i
 
 // Compile (without a GPU) and store in the on-disk cache the specialisation of `h`;
 // returns false with the reason in `note` when the run-time compiler is missing or fails.
-bool nr_prepare(const cbh::NrCode& h, std::string* note, bool learned = false);
+bool nr_prepare(const cbh::NrCode& h, std::string* note, bool learned = false, int rule = 1);
 
 }  // namespace cbk
