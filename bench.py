@@ -62,11 +62,11 @@ ALGO_BYTES = E * 4 + (K_INFO + 7) // 8 + 4
 # DRAM bytes (read + write) of the decoder per codeword at 20 iterations, and the
 # warp-instructions it issues per codeword and iteration, from one ncu capture of a
 # 2048-codeword launch of the decoder compiled for this code's lifting
-# (profiles/decode_c2_f32.md: 207,899,904 + 71,494,656 B, smsp__inst_executed.sum =
-# 3,453,805,408); the persistent grid keeps the same 304 state slots at any batch, so both
+# (profiles/decode_c2_f32.md: 207,803,136 + 81,634,560 B, smsp__inst_executed.sum =
+# 3,337,917,248); the persistent grid keeps the same 304 state slots at any batch, so both
 # scale by codewords
-DRAM_BYTES_PER_CODEWORD = (207_899_904 + 71_494_656) / 2048
-WARP_INST_PER_CODEWORD_ITERATION = 3_453_805_408 / (2048 * 20)
+DRAM_BYTES_PER_CODEWORD = (207_803_136 + 81_634_560) / 2048
+WARP_INST_PER_CODEWORD_ITERATION = 3_337_917_248 / (2048 * 20)
 WORKLOAD = ("5G NR LDPC BG1 Z=384 K'=8448 E=25344 (rate 1/3), Gray 16-QAM, AWGN Eb/N0 0:0.25:2 dB, "
             "max-log LLRs, layered NMS alpha=0.75, <=20 iterations + syndrome stop, 8192 codewords/launch")
 # a point at the code's waterfall (FER about 0.13; the grid above sits at FER 1)

@@ -757,8 +757,8 @@ cb_status nms_buffers(cb_nms* h, int64_t n, bool train) {
 // Then `w` receives a host copy of the weights (scales then offsets).
 // The graph-specialised learned kernel serves evaluation when the code's plain decoder is
 // the graph-specialised one, the weights are shared and fit the launch parameters, and
-// the lifting is large: the same results as the table-driven learned decoder, at 1.44x
-// the plain decoder's time per iteration on BG1 Z = 384 (C5 at its FER 1e-3 point: 9.2 ms
+// the lifting is large: the same results as the table-driven learned decoder, at 1.40x
+// the plain decoder's time per iteration on BG1 Z = 384 (C5 at its FER 1e-3 point: 8.5 ms
 // for 8192 frames, 13.8 ms with the table-driven kernel).  With Z = 52 (C4) a dozen CTAs
 // share an SM, and with its weights read from the launch parameters it ran 2.5-3.4x the
 // plain decoder's time per iteration, slower than the table-driven kernel with its weights

@@ -199,7 +199,7 @@ struct LearnedRowW {
   int s0, stride, roff;
   __device__ __forceinline__ float mag(const float* al, const float* be, int e, float m) const {
     const int i = (s0 + e) * stride + roff;
-    const float am = __fsub_rn(__fmul_rn(al[i], m), be[i]);
+    const float am = __fmaf_rn(al[i], m, -be[i]);
     return am > 0.f ? am : 0.f;
   }
 };

@@ -262,13 +262,14 @@ __device__ __forceinline__ void nr_row(unsigned char* post, const NrArgs& a, int
   nm = (sm << 8) | i1;
 }
 
-// The learned message magnitude max(alpha m - beta, 0), rounded as the training forward
-// (nms_learned.cu) and LearnedRowW (decode_common.cuh) compute it.  fmaxf agrees with
-// their `am > 0 ? am : 0` except perhaps on the sign of a zero from am = -0; a message of
-// magnitude zero adds or subtracts zero whatever its sign, so the posteriors are the
-// same bits (the sign bit kept for it only ever multiplies that zero again).
+// The learned message magnitude max(alpha m - beta, 0), alpha m - beta rounded once (a
+// fused multiply-add) as the training forward (nms_learned.cu) and LearnedRowW
+// (decode_common.cuh) compute it.  fmaxf agrees with their `am > 0 ? am : 0` except
+// perhaps on the sign of a zero from am = -0; a message of magnitude zero adds or
+// subtracts zero whatever its sign, so the posteriors are the same bits (the sign bit kept
+// for it only ever multiplies that zero again).
 __device__ __forceinline__ float learned_mag(float al, float be, float m) {
-  return fmaxf(__fsub_rn(__fmul_rn(al, m), be), 0.f);
+  return fmaxf(__fmaf_rn(al, m, -be), 0.f);
 }
 
 // One lifted row of the learned min-sum (row_update_learned of decode_common.cuh, with

@@ -4,7 +4,8 @@
 // min-sum is its special case alpha = 0.75, beta = 0 and remains its fallback.
 //
 // Check message at iteration t, edge e of a row (the row's other edges k != e):
-//   y_e = s_e * max(alpha[t, e] * m_e - beta[t, e], 0),
+//   y_e = s_e * max(alpha[t, e] * m_e - beta[t, e], 0)  (the product and the difference
+//   rounded once, as one fused multiply-add),
 //   s_e = prod sign(x_k), m_e = min |x_k|, x_k = post[v_k] - c2v_k (ldpc.rs:468-491),
 // then post[v_e] = x_e + y_e and c2v_e = y_e.  Weights are indexed [t][entry][r] (one per
 // lifted edge) or [t][entry] (one per base-graph edge, shared across Z); the edge
@@ -77,7 +78,7 @@ __device__ __forceinline__ void learned_row_fwd(const LearnedArgs& a, float* pos
   for (int e = 0; e < D; e++) {
     const size_t w = weight_index(a, t, s0 + e, r);
     float m = e == i1 ? m2 : m1;
-    float am = __fsub_rn(__fmul_rn(a.alpha[w], m), a.beta[w]);
+    float am = __fmaf_rn(a.alpha[w], m, -a.beta[w]);
     float mag = am > 0.f ? am : 0.f;
     bool neg = (par ^ (uint32_t)(x[e] < 0.f)) & 1u;
     float y = neg ? -mag : mag;
@@ -123,7 +124,7 @@ __device__ __forceinline__ void learned_row_bwd(const LearnedArgs& a, float* gp,
     const size_t ed = (size_t)(s0 + e) * z + r;
     float m = e == i1 ? m2 : m1;
     float al = a.alpha[w];
-    float am = al * m - a.beta[w];
+    float am = __fmaf_rn(al, m, -a.beta[w]);
     bool neg = (par ^ (uint32_t)(x[e] < 0.f)) & 1u;
     float gy = gp[off[e]] + gc[ed];
     float ga = am > 0.f ? (neg ? -gy : gy) : 0.f;

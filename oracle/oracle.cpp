@@ -934,7 +934,7 @@ static double learned_frame(const Learned& L, const R* full_llr, const uint8_t* 
           R m = i == i1 ? m2 : m1;
           bool neg = par ^ (x[i] < 0);
           size_t w = widx(L, t, L.lstart[Ly] + i, r);
-          R a = (R)alpha[w] * m - (R)beta[w];
+          R a = std::fma((R)alpha[w], m, -(R)beta[w]);
           R mag = a > 0 ? a : (R)0;
           R y = neg ? -mag : mag;
           c2v[e0 + i] = y;
@@ -997,7 +997,7 @@ static double learned_frame(const Learned& L, const R* full_llr, const uint8_t* 
           R m = i == i1 ? m2 : m1;
           bool neg = par ^ (x[i] < 0);
           size_t w = widx(L, t, L.lstart[Ly] + i, r);
-          R a = (R)alpha[w] * m - (R)beta[w];
+          R a = std::fma((R)alpha[w], m, -(R)beta[w]);
           R g_y = gp[v] + gc[e0 + i];
           R g_a = a > 0 ? (neg ? -g_y : g_y) : (R)0;
           ga[w] += (double)(g_a * m);
