@@ -289,6 +289,7 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
   T* out = a.llr_out;
   if (sizeof(T) == 8) {
     const double sd = __dsqrt_rn(sigma2);
+    const double inv_s2 = __drcp_rn(sigma2);  // RN(1 / sigma2), for neg_div_by
     for (int s = s0; s < s1; s++) {
       double nre, nim;
       complex_gaussian_f64(r, nre, nim);
@@ -296,7 +297,7 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
       const double yre = __dadd_rn(pts[2 * li], __dmul_rn(nre, sd));
       const double yim = __dadd_rn(pts[2 * li + 1], __dmul_rn(nim, sd));
       const int t0 = s * a.mbits;
-      demap_f64(pts, a.m, a.mbits, a.log_m, a.exact != 0, yre, yim, sigma2, c.e - t0,
+      demap_f64(pts, a.m, a.mbits, a.log_m, a.exact != 0, yre, yim, sigma2, inv_s2, c.e - t0,
                 [&](int o, double v) { out[t0 + o] = (T)v; });
     }
   } else {

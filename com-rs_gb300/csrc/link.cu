@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(NT) link_gen_kernel(const __grid_constant__ Li
       cbd::Xoshiro r = cbd::stream(a.seed, a.name_hash, a.cond, t_idx);
       cbd::xoshiro_jump(r, a.jumps + 4 * (NT + tid));
       const double sd = __dsqrt_rn(sigma2);
+      const double inv_s2 = __drcp_rn(sigma2);  // RN(1 / sigma2), for neg_div_by
       for (int s = s0; s < s1; s++) {
         double nre, nim;
         complex_gaussian_f64(r, nre, nim);
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(NT) link_gen_kernel(const __grid_constant__ Li
         ys[2 * s] = yre;
         ys[2 * s + 1] = yim;
         const int t0 = s * a.mbits;
-        demap_f64(pts, a.m, a.mbits, a.log_m, a.exact != 0, yre, yim, sigma2, nb - t0, [&](int o, double v) {
+        demap_f64(pts, a.m, a.mbits, a.log_m, a.exact != 0, yre, yim, sigma2, inv_s2, nb - t0, [&](int o, double v) {
           const int t = t0 + o;
           const int pos = a.perm ? a.perm[t] : t;
           if (llr32) llr32[pos] = (float)v;
