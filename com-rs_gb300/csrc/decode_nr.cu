@@ -414,8 +414,9 @@ cudaError_t set_smem(const NrKernel& k, size_t smem, int device) {
 }
 }  // namespace
 
-int nr_grid_size(const NrKernel& k, const cbh::NrCode& h, int device) {
-  const size_t smem = nr_smem(h);
+namespace {
+// resident CTAs of a kernel of this code's block size with `smem` bytes of shared memory
+int grid_for(const NrKernel& k, const cbh::NrCode& h, int device, size_t smem) {
   if (set_smem(k, smem, device) != cudaSuccess) return 0;
   int per_sm = 0, sms = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, ((h.z + 31) / 32) * 32, smem) != cudaSuccess)
@@ -423,36 +424,34 @@ int nr_grid_size(const NrKernel& k, const cbh::NrCode& h, int device) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   return per_sm * sms;
 }
+}  // namespace
 
-cudaError_t nr_launch(const NrKernel& k, const cbn::NrArgs& a, int grid, cudaStream_t stream) {
-  const size_t smem = cbn::nr_smem_bytes(a.n_full, a.z, a.rows, a.n_entries);
+int nr_grid_size(const NrKernel& k, const cbh::NrCode& h, int device) { return grid_for(k, h, device, nr_smem(h)); }
+
+int nr_learned_grid_size(const NrKernel& k, const cbh::NrCode& h, int device) {
+  return grid_for(k, h, device, cbn::nr_learned_smem_bytes(h.n_full, h.z, h.rows_n, (int)h.entry_col.size()));
+}
+
+namespace {
+// one launch of the decoder for lifting z with `smem` bytes of shared memory; `params`
+// points at its launch parameters (NrArgs or NrLearnedArgs)
+cudaError_t launch_with(const NrKernel& k, const void* params, int z, size_t smem, int grid, cudaStream_t stream) {
   int device = 0;
   cudaGetDevice(&device);
   cudaError_t e = set_smem(k, smem, device);
   if (e != cudaSuccess) return e;
-  void* args[] = {(void*)&a};
-  return cudaLaunchKernel(k.fn, dim3(grid), dim3(((a.z + 31) / 32) * 32), args, smem, stream);
+  void* args[] = {const_cast<void*>(params)};
+  return cudaLaunchKernel(k.fn, dim3(grid), dim3(((z + 31) / 32) * 32), args, smem, stream);
 }
+}  // namespace
 
-int nr_learned_grid_size(const NrKernel& k, const cbh::NrCode& h, int device) {
-  const size_t smem = cbn::nr_learned_smem_bytes(h.n_full, h.z, h.rows_n, (int)h.entry_col.size());
-  if (set_smem(k, smem, device) != cudaSuccess) return 0;
-  int per_sm = 0, sms = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, ((h.z + 31) / 32) * 32, smem) != cudaSuccess)
-    return 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  return per_sm * sms;
+cudaError_t nr_launch(const NrKernel& k, const cbn::NrArgs& a, int grid, cudaStream_t stream) {
+  return launch_with(k, &a, a.z, cbn::nr_smem_bytes(a.n_full, a.z, a.rows, a.n_entries), grid, stream);
 }
 
 cudaError_t nr_learned_launch(const NrKernel& k, const cbn::NrLearnedArgs& la, int grid, cudaStream_t stream) {
   const cbn::NrArgs& a = la.a;
-  const size_t smem = cbn::nr_learned_smem_bytes(a.n_full, a.z, a.rows, a.n_entries);
-  int device = 0;
-  cudaGetDevice(&device);
-  cudaError_t e = set_smem(k, smem, device);
-  if (e != cudaSuccess) return e;
-  void* args[] = {(void*)&la};
-  return cudaLaunchKernel(k.fn, dim3(grid), dim3(((a.z + 31) / 32) * 32), args, smem, stream);
+  return launch_with(k, &la, a.z, cbn::nr_learned_smem_bytes(a.n_full, a.z, a.rows, a.n_entries), grid, stream);
 }
 
 }  // namespace cbk
