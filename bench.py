@@ -67,6 +67,10 @@ ALGO_BYTES = E * 4 + (K_INFO + 7) // 8 + 4
 # scale by codewords
 DRAM_BYTES_PER_CODEWORD = (207_803_136 + 81_634_560) / 2048
 WARP_INST_PER_CODEWORD_ITERATION = 3_337_917_248 / (2048 * 20)
+# edges of the lifted graph (BG1's 316 entries x Z) and the layered min-sum's algorithmic
+# operations per edge and iteration
+N_EDGES = 316 * 384
+OPS_PER_EDGE_ITERATION = 10
 WORKLOAD = ("5G NR LDPC BG1 Z=384 K'=8448 E=25344 (rate 1/3), Gray 16-QAM, AWGN Eb/N0 0:0.25:2 dB, "
             "max-log LLRs, layered NMS alpha=0.75, <=20 iterations + syndrome stop, 8192 codewords/launch")
 # a point at the code's waterfall (FER about 0.13; the grid above sits at FER 1)
@@ -299,6 +303,13 @@ def run_ours(args, rank, world, local_rank):
     roofline["issue"] = {"achieved": issue_achieved, "peak": issue_peak, "unit": "warp-inst/s",
                          "frac": issue_achieved / issue_peak,
                          "source": "warp-instructions per codeword-iteration from an ncu capture of 2048 codewords"}
+    # the algorithmic-ops fraction: 10 operations per edge and iteration of the layered
+    # min-sum (subtraction, magnitude, two compare-selects, sign product, output choice,
+    # scaling, sign, addition, syndrome bit), against the issue peak in thread-instructions
+    ops_achieved = OPS_PER_EDGE_ITERATION * N_EDGES * B * float(np.mean(dec_it)) / (dec * 1e-3)
+    roofline["ops"] = {"achieved": ops_achieved, "peak": 32 * issue_peak, "unit": "thread-op/s",
+                       "frac": ops_achieved / (32 * issue_peak), "ops_per_edge_iteration": OPS_PER_EDGE_ITERATION,
+                       "edges": N_EDGES}
 
     # end to end through the public C ABI: per-frame records to pinned host memory
     host = torch.empty(B * 8, dtype=torch.uint8, pin_memory=True)
