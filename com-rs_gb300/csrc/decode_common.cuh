@@ -51,14 +51,13 @@ __device__ __forceinline__ void row_update(T* __restrict__ post, const uint32_t*
     // f64 on the integer pipes: the posteriors and messages are never -0.0 or NaN, so
     // `l < 0` is the sign bit, and the order of non-negative doubles is that of their
     // bit patterns; only the subtractions and additions stay on the FP64 pipe
-    const long long kAbs = 0x7fffffffffffffffll;
     par = (uint32_t)((unsigned long long)__double_as_longlong(x[0]) >> 63);
-    long long b1 = __double_as_longlong(x[0]) & kAbs, b2 = 0x7ff0000000000000ll;
+    long long b1 = abs_bits(__double_as_longlong(x[0])), b2 = 0x7ff0000000000000ll;
 #pragma unroll
     for (int e = 1; e < D; e++) {
       const long long bx = __double_as_longlong(x[e]);
       par ^= (uint32_t)((unsigned long long)bx >> 63);
-      const long long av = bx & kAbs;
+      const long long av = abs_bits(bx);
       const bool lt = av < b1;
       b2 = lt ? b1 : (av < b2 ? av : b2);
       b1 = lt ? av : b1;

@@ -37,6 +37,15 @@ __device__ __forceinline__ double mul_rn<double>(double a, double b) { return __
 template <>
 __device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
 
+// The bit pattern of |x| from that of a double x: the AND as inline PTX, opaque to the
+// compiler's recognition of `bits & 0x7fff...` as fabs, whose result it then forms on the
+// FP64 pipe when the consumer is an integer comparison
+__device__ __forceinline__ long long abs_bits(long long b) {
+  long long r;
+  asm("and.b64 %0, %1, 0x7fffffffffffffff;" : "=l"(r) : "l"(b));
+  return r;
+}
+
 template <typename T>
 __device__ __forceinline__ T infinity();
 template <>

@@ -133,12 +133,12 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, int pos, 
     // s * mag with s = +-1 is mag with its sign bit flipped.  The scaled magnitudes are
     // the same for every edge, so they are computed once.  The results are the same
     // bits as the branch below.
-    const long long kAbs = 0x7fffffffffffffffll, kInf = 0x7ff0000000000000ll;
+    const long long kInf = 0x7ff0000000000000ll;
     int neg = 0, i1 = 0;
     long long b1 = kInf, b2 = kInf;
     for (int i = 0; i < d; i++) {
       const long long bl = __double_as_longlong((double)sub_rn(post[es.var(i)], msg[es.slot(i)]));
-      const long long a = bl & kAbs;
+      const long long a = abs_bits(bl);
       neg ^= (int)(bl < 0 && a != 0 && a <= kInf);
       if (a < b1) {
         b2 = b1;
@@ -154,7 +154,7 @@ __device__ __forceinline__ void check_row(const SparseDev& c, int row, int pos, 
     for (int i = 0; i < d; i++) {
       const int e = es.slot(i), v = es.var(i);
       const T l = sub_rn(post[v], msg[e]);
-      const long long bl = __double_as_longlong((double)l), a = bl & kAbs;
+      const long long bl = __double_as_longlong((double)l), a = abs_bits(bl);
       const int sneg = neg ^ (int)(bl < 0 && a != 0 && a <= kInf);
       const long long mb = __double_as_longlong((double)(i == i1 ? n2 : n1));
       const T o = (T)__longlong_as_double(mb ^ ((long long)sneg << 63));
@@ -296,12 +296,12 @@ __device__ __forceinline__ void check_row_warp(const SparseDev& c, int row, T* p
   } else if (sizeof(T) == 8) {
     // f64: the integer forms of check_row's f64 min-sum (the same bits); the reduction
     // keeps the first index among equal minima, as the strict `<` of the sequential loop
-    const long long kAbs = 0x7fffffffffffffffll, kInf = 0x7ff0000000000000ll;
+    const long long kInf = 0x7ff0000000000000ll;
     int neg = 0, i1 = 0x7fffffff;
     long long b1 = kInf, b2 = kInf;
     for (int e = e0 + lane; e < e1; e += 32) {
       const long long bl = __double_as_longlong((double)sub_rn(post[c.vars[e]], msg[e]));
-      const long long a = bl & kAbs;
+      const long long a = abs_bits(bl);
       neg ^= (int)(bl < 0 && a != 0 && a <= kInf);
       if (a < b1) {
         b2 = b1;
@@ -329,7 +329,7 @@ __device__ __forceinline__ void check_row_warp(const SparseDev& c, int row, T* p
     for (int e = e0 + lane; e < e1; e += 32) {
       const int v = c.vars[e];
       const T l = sub_rn(post[v], msg[e]);
-      const long long bl = __double_as_longlong((double)l), a = bl & kAbs;
+      const long long bl = __double_as_longlong((double)l), a = abs_bits(bl);
       const int sneg = neg ^ (int)(bl < 0 && a != 0 && a <= kInf);
       const long long mb = __double_as_longlong((double)((e - e0) == i1 ? n2 : n1));
       const T o = (T)__longlong_as_double(mb ^ ((long long)sneg << 63));
