@@ -44,6 +44,13 @@ __device__ __forceinline__ double fma_rn(double a, double b, double c) { return 
 __device__ __forceinline__ double rcp(double a) { return __drcp_rn(a); }
 __device__ __forceinline__ uint64_t bits(double x) { return (uint64_t)__double_as_longlong(x); }
 __device__ __forceinline__ double from_bits(uint64_t b) { return __longlong_as_double((long long)b); }
+// the bits of |x| by an AND in inline PTX (written in C++, the compiler turns the AND into
+// fabs and forms |x| with an FP64 instruction for the integer comparison that follows)
+__device__ __forceinline__ uint64_t abs_bits(uint64_t b) {
+  uint64_t r;
+  asm("and.b64 %0, %1, 0x7fffffffffffffff;" : "=l"(r) : "l"(b));
+  return r;
+}
 __device__ __forceinline__ double tab(int j, int k) { return __ldg(&LOGTAB[j][k]); }
 #else
 inline double add(double a, double b) { return a + b; }
@@ -56,6 +63,7 @@ inline uint64_t bits(double x) {
   std::memcpy(&b, &x, 8);
   return b;
 }
+inline uint64_t abs_bits(uint64_t b) { return b & 0x7fffffffffffffffull; }
 inline double from_bits(uint64_t b) {
   double x;
   std::memcpy(&x, &b, 8);
@@ -68,7 +76,7 @@ inline double tab(int j, int k) { return LOGTAB[j][k]; }
 AT2_HD double twice_atanh(double p, double bound) {
   const uint64_t sign = bits(p) & 0x8000000000000000ull;
   // a = min(|p|, bound): non-negative doubles order as their bit patterns
-  uint64_t ab = bits(p) & 0x7fffffffffffffffull;
+  uint64_t ab = abs_bits(bits(p));
   const uint64_t bb = bits(bound);
   ab = ab < bb ? ab : bb;
   const double a = from_bits(ab);
