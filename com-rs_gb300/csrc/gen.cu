@@ -130,7 +130,9 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
   uint8_t* lab = cw + c.n_full;
   uint8_t* pad = lab + n_sym;  // padding bits (< mbits)
   __shared__ double s_sigma2;
-  __shared__ unsigned int s_hist[256];
+  // f32 frames: the label histogram; f64 frames: the labels' energies
+  __shared__ double s_tab[256];
+  unsigned int* s_hist = reinterpret_cast<unsigned int*>(s_tab);
   const uint64_t fidx = a.frame_index;
 
   for (int i = tid; i < 2 * a.m; i += NT) pts[i] = a.points[i];
@@ -254,12 +256,10 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
   // ---- measured power (com-math lib.rs:146-148)
   if (sizeof(T) == 8) {
     // f64 frames: summed in symbol order, as the reference
+    label_energies(pts, a.m, s_tab, tid, NT);
+    __syncthreads();
     if (tid == 0) {
-      double e = 0.0;
-      for (int s = 0; s < n_sym; s++) {
-        double re = pts[2 * lab[s]], im = pts[2 * lab[s] + 1];
-        e = __dadd_rn(e, __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
-      }
+      const double e = energy_sum(lab, n_sym, s_tab);
       double p = __ddiv_rn(__dadd_rn(0.0, e), (double)n_sym);
       s_sigma2 = __ddiv_rn(p, a.b_ebn0);
     }

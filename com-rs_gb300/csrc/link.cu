@@ -21,6 +21,8 @@
 // each thread jumps to its chunk of the stream with a precomputed polynomial.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.h"
 #include "qam_f64.cuh"
 
@@ -35,6 +37,12 @@ __device__ __forceinline__ int grid_cell(double x, double x0, double step, int s
   return (int)fmin(fmax(c, 0.0), (double)(side - 1));
 }
 
+// byte offset of the generator's tail buffers (8-byte aligned, after the labels and
+// padding bits)
+__host__ __device__ inline size_t link_gen_tail_offset(int m, int n_sym, int mbits) {
+  return ((size_t)2 * m * 8 + (size_t)2 * n_sym * 8 + (size_t)n_sym + (size_t)mbits + 7) & ~(size_t)7;
+}
+
 __global__ void __launch_bounds__(NT) link_gen_kernel(const __grid_constant__ LinkGenArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t trial = blockIdx.x;
@@ -43,17 +51,20 @@ __global__ void __launch_bounds__(NT) link_gen_kernel(const __grid_constant__ Li
   const int kb = a.k * a.blocks, nb = a.n * a.blocks;
   const int n_sym = (nb + a.n_pad) / a.mbits;
   const int wk = (a.k + 31) >> 5;  // packed words of one block's information bits
-  // shared layout: points (2m doubles) | received samples (2 n_sym doubles) | packed
-  // information words (blocks x wk) | payload bytes (kb) | coded bytes (nb) | labels
-  // (n_sym) | padding bits
+  // shared layout: points (2m doubles) | received samples (2 n_sym doubles) | labels
+  // (n_sym) | padding bits | (8-byte aligned) packed information words (blocks x wk) |
+  // payload bytes (kb) | coded bytes (nb); the received samples' energies (n_sym doubles)
+  // take the place of the last three once the labels are formed
   double* pts = reinterpret_cast<double*>(smem);
   double* ys = pts + 2 * a.m;
-  uint32_t* uw = reinterpret_cast<uint32_t*>(ys + 2 * n_sym);
+  uint8_t* lab = reinterpret_cast<uint8_t*>(ys + 2 * n_sym);
+  uint8_t* pad = lab + n_sym;
+  uint32_t* uw = reinterpret_cast<uint32_t*>(smem + link_gen_tail_offset(a.m, n_sym, a.mbits));
   uint8_t* pay = reinterpret_cast<uint8_t*>(uw + a.blocks * wk);
   uint8_t* cw = pay + kb;
-  uint8_t* lab = cw + nb;
-  uint8_t* pad = lab + n_sym;
+  double* yen = reinterpret_cast<double*>(uw);
   __shared__ double s_sigma2, s_ex, s_gain;
+  __shared__ double s_en[256];  // the labels' energies
   __shared__ unsigned int s_err;
   const uint64_t t_idx = a.first_trial + (uint64_t)trial;
 
@@ -109,12 +120,10 @@ __global__ void __launch_bounds__(NT) link_gen_kernel(const __grid_constant__ Li
   }
   __syncthreads();
   // ---- measured power, summed in symbol order
+  label_energies(pts, a.m, s_en, tid, NT);
+  __syncthreads();
   if (tid == 0) {
-    double e = 0.0;
-    for (int s = 0; s < n_sym; s++) {
-      const double re = pts[2 * lab[s]], im = pts[2 * lab[s] + 1];
-      e = __dadd_rn(e, __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
-    }
+    const double e = energy_sum(lab, n_sym, s_en);
     s_ex = e;
     s_sigma2 = __ddiv_rn(__ddiv_rn(__dadd_rn(0.0, e), (double)n_sym), a.b_ebn0);
   }
@@ -139,6 +148,7 @@ __global__ void __launch_bounds__(NT) link_gen_kernel(const __grid_constant__ Li
         const double yim = __dadd_rn(pts[2 * li + 1], __dmul_rn(nim, sd));
         ys[2 * s] = yre;
         ys[2 * s + 1] = yim;
+        yen[s] = __dadd_rn(__dmul_rn(yre, yre), __dmul_rn(yim, yim));
         const int t0 = s * a.mbits;
         demap_f64(pts, a.m, a.mbits, a.log_m, a.exact != 0, yre, yim, sigma2, inv_s2, nb - t0, [&](int o, double v) {
           const int t = t0 + o;
@@ -150,11 +160,13 @@ __global__ void __launch_bounds__(NT) link_gen_kernel(const __grid_constant__ Li
     }
   }
   __syncthreads();
-  // ---- metric ber: the gain sqrt(energy(x) / energy(y)), both summed in symbol order
+  // ---- metric ber: the gain sqrt(energy(x) / energy(y)), both summed in symbol order;
+  // each |y|^2 was formed by the thread that drew y, so the sequential chain on one lane is
+  // one FP64 addition per symbol
   if (tid == 0) {
     double e = 0.0;
-    for (int s = 0; s < n_sym; s++)
-      e = __dadd_rn(e, __dadd_rn(__dmul_rn(ys[2 * s], ys[2 * s]), __dmul_rn(ys[2 * s + 1], ys[2 * s + 1])));
+#pragma unroll 8
+    for (int s = 0; s < n_sym; s++) e = __dadd_rn(e, yen[s]);
     const double ey = __dadd_rn(0.0, e), ex = __dadd_rn(0.0, s_ex);
     s_gain = ey > 0.0 ? __dsqrt_rn(__ddiv_rn(ex, ey)) : 1.0;
   }
@@ -217,8 +229,8 @@ __global__ void __launch_bounds__(NT) link_count_kernel(const __grid_constant__ 
 
 size_t link_gen_smem_bytes(int m, int mbits, int k, int n, int blocks, int n_pad) {
   const int nb = n * blocks, n_sym = (nb + n_pad) / mbits, wk = (k + 31) / 32;
-  return (size_t)2 * m * 8 + (size_t)2 * n_sym * 8 + (size_t)blocks * wk * 4 + (size_t)k * blocks + nb + n_sym +
-         (size_t)mbits + 16;
+  const size_t tail = (size_t)blocks * wk * 4 + (size_t)k * blocks + nb;
+  return link_gen_tail_offset(m, n_sym, mbits) + std::max(tail, (size_t)n_sym * 8) + 16;
 }
 
 cudaError_t launch_link_gen(const LinkGenArgs& a, cudaStream_t stream) {
