@@ -110,6 +110,22 @@ def test_qam_is_gray_and_unit_energy(O):
     assert np.allclose(pts, [(-1 + 1j) * s, (1 + 1j) * s, (-1 - 1j) * s, (1 - 1j) * s])
 
 
+def test_qam_label_bits_split_by_dimension(O):
+    # the premise of the GPU's f64 max-log demapper (half minima per dimension): in the
+    # reference's Gray square QAM the last log2(side) label bits fix the real part and the
+    # first log2(side) bits the imaginary part, the same doubles for every such label
+    for m in (4, 16, 64, 256):
+        pts, _ = O.qam(m)
+        side = int(round(np.sqrt(m)))
+        lab = np.arange(m)
+        re, im = pts.real.view(np.uint64), pts.imag.view(np.uint64)
+        for low in range(side):
+            assert len(set(re[(lab % side) == low].tolist())) == 1
+        for high in range(side):
+            assert len(set(im[(lab // side) == high].tolist())) == 1
+        assert len(set(re.tolist())) == side and len(set(im.tolist())) == side
+
+
 def test_demapper_max_log_matches_brute_force(O):
     rng = np.random.default_rng(1)
     for m in (4, 16, 64):
