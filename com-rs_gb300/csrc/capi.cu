@@ -312,14 +312,69 @@ cb_status trial_device_impl(cb_code* c, int m, uint64_t seed, uint64_t name_hash
   return decode_device_impl<T>(c, llr_dev, n, nullptr, nullptr, nullptr, info_dev, results, s);
 }
 
+// the decisions (packed to bytes), a posteriori LLRs and iteration counts of frames
+// [done, done + cnt) from the device buffers to the caller's host buffers, on the code's
+// stream
+template <typename T>
+cb_status copy_back(cb_code* c, int64_t done, int64_t cnt, int wpf, int bpf, uint8_t* bits, T* app, int32_t* iters) {
+  if (bits) {
+    if (bpf == wpf * 4) {
+      CB_CUDA(c, cudaMemcpyAsync(bits + (size_t)done * bpf, c->d_bits, (size_t)cnt * bpf, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    } else {
+      c->h_words.resize((size_t)cnt * wpf);
+      CB_CUDA(c, cudaMemcpyAsync(c->h_words.data(), c->d_bits, (size_t)cnt * wpf * 4, cudaMemcpyDeviceToHost,
+                                 c->stream));
+      CB_CUDA(c, cudaStreamSynchronize(c->stream));
+      for (int64_t f = 0; f < cnt; f++) std::memcpy(bits + (size_t)(done + f) * bpf, &c->h_words[(size_t)f * wpf], bpf);
+    }
+  }
+  if (app)
+    CB_CUDA(c, cudaMemcpyAsync(app + (size_t)done * c->host.k_info, c->d_app, (size_t)cnt * c->host.k_info * sizeof(T),
+                               cudaMemcpyDeviceToHost, c->stream));
+  if (iters) CB_CUDA(c, cudaMemcpyAsync(iters + done, c->d_iters, (size_t)cnt * 4, cudaMemcpyDeviceToHost, c->stream));
+  return CB_OK;
+}
+
+// The device address of a host buffer the GPU reads in place (page-locked memory, mapped
+// under unified addressing), or nullptr
+template <typename T>
+const T* mapped_host(const T* p) {
+  cudaPointerAttributes pa;
+  if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return pa.type == cudaMemoryTypeHost && pa.devicePointer ? static_cast<const T*>(pa.devicePointer) : nullptr;
+}
+
 template <typename T>
 cb_status decode_host_impl(cb_code* c, const T* llr, int64_t n, uint8_t* bits, T* app, int32_t* iters) {
+  const int wpf = (c->host.k_info + 31) / 32;
+  const int bpf = (c->host.k_info + 7) / 8;
+  // Page-locked host LLRs: the decoder reads them where they are (over NVLink-C2C on a
+  // Grace host), one launch per chunk of frames with no staging copy; only the decisions,
+  // a posteriori LLRs and counts come back by copies.
+  if (const T* dev_llr = mapped_host(llr)) {
+    const int64_t chunk = std::min<int64_t>(n, chunk_frames(c));
+    CB_CUDA(c, grow(c->d_bits, c->bits_cap, (size_t)chunk * wpf * 4));
+    if (app) CB_CUDA(c, grow(c->d_app, c->app_cap, (size_t)chunk * c->host.k_info * sizeof(T)));
+    if (iters) CB_CUDA(c, grow(c->d_iters, c->iters_cap, (size_t)chunk * 4));
+    for (int64_t done = 0; done < n; done += chunk) {
+      const int64_t cnt = std::min(chunk, n - done);
+      cb_status st = decode_device_impl<T>(c, dev_llr + (size_t)done * c->host.e, cnt, c->d_bits,
+                                           app ? reinterpret_cast<T*>(c->d_app) : nullptr,
+                                           iters ? c->d_iters : nullptr, nullptr, nullptr, c->stream);
+      if (st) return st;
+      if (cb_status rs = copy_back(c, done, cnt, wpf, bpf, bits, app, iters)) return rs;
+    }
+    CB_CUDA(c, cudaStreamSynchronize(c->stream));
+    return CB_OK;
+  }
   // Host LLRs in chunks: chunk i + 1 is copied on the copy stream while chunk i decodes on
   // the code's stream, through two device buffers (an event per buffer marks its copy
   // done, another the decode that read it); decisions and counts go back on the decode
   // stream.  Each chunk holds at least one persistent grid's worth of codewords.
-  const int wpf = (c->host.k_info + 31) / 32;
-  const int bpf = (c->host.k_info + 7) / 8;
   const size_t per = (size_t)c->host.e * sizeof(T);
   const int64_t grid = std::max(1, c->decode_grid);
   const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(chunk_frames(c) / 2,
@@ -343,24 +398,7 @@ cb_status decode_host_impl(cb_code* c, const T* llr, int64_t n, uint8_t* bits, T
                                          iters ? c->d_iters : nullptr, nullptr, nullptr, c->stream);
     if (st) return st;
     CB_CUDA(c, cudaEventRecord(c->ev_read[half], c->stream));
-    if (bits) {
-      if (bpf == wpf * 4) {
-        CB_CUDA(c, cudaMemcpyAsync(bits + (size_t)done * bpf, c->d_bits, (size_t)cnt * bpf, cudaMemcpyDeviceToHost,
-                                   c->stream));
-      } else {
-        c->h_words.resize((size_t)cnt * wpf);
-        CB_CUDA(c, cudaMemcpyAsync(c->h_words.data(), c->d_bits, (size_t)cnt * wpf * 4, cudaMemcpyDeviceToHost,
-                                   c->stream));
-        CB_CUDA(c, cudaStreamSynchronize(c->stream));
-        for (int64_t f = 0; f < cnt; f++)
-          std::memcpy(bits + (size_t)(done + f) * bpf, &c->h_words[(size_t)f * wpf], bpf);
-      }
-    }
-    if (app)
-      CB_CUDA(c, cudaMemcpyAsync(app + (size_t)done * c->host.k_info, c->d_app,
-                                 (size_t)cnt * c->host.k_info * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
-    if (iters)
-      CB_CUDA(c, cudaMemcpyAsync(iters + done, c->d_iters, (size_t)cnt * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (cb_status rs = copy_back(c, done, cnt, wpf, bpf, bits, app, iters)) return rs;
   }
   CB_CUDA(c, cudaStreamSynchronize(c->stream));
   return CB_OK;

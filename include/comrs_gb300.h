@@ -115,7 +115,9 @@ cb_status cb_encode(cb_code* code, const uint8_t* info, int64_t n_frames, uint8_
 /* Decode n_frames blocks of E channel LLRs (double for CB_F64, float for CB_F32),
  * host buffers.  bits: n_frames x ceil(K'/8) bytes, packed LSB first (optional);
  * app: n_frames x K' a posteriori LLRs of the information bits (optional);
- * iterations: n_frames int32 (optional). */
+ * iterations: n_frames int32 (optional).  Page-locked LLRs (cudaHostAlloc,
+ * cudaHostRegister) are read by the decoder in place; others are copied to the device in
+ * chunks that overlap the decoding.  The results are the same. */
 cb_status cb_decode(cb_code* code, const void* llr, int64_t n_frames, uint8_t* bits, void* app,
                     int32_t* iterations);
 

@@ -216,6 +216,27 @@ def test_concurrent_callers_on_one_code_object(cb):
         assert np.array_equal(wa.view(np.uint32), ga.view(np.uint32))
 
 
+@pytest.mark.parametrize("spec", [dict(k=8448, e=25344, bg=1, z=384, n=600, m=16, eb=2.6, precision="f32"),
+                                  dict(k=8448, e=25344, bg=1, z=384, n=300, m=16, eb=2.6, precision="f64"),
+                                  dict(k=520, e=1040, bg=2, z=52, n=70000, m=4, eb=1.5, precision="f32")],
+                         ids=["c2_f32", "c2_f64", "c1_f32_two_chunks"])
+def test_host_decode_reads_page_locked_llrs_in_place(cb, spec):
+    # page-locked host LLRs are read by the decoder where they are, without staging copies
+    # (C1: two launches of 65,536 and 4,464 frames): the same decisions, a posteriori LLRs
+    # and iterations as from pageable memory
+    torch = pytest.importorskip("torch")
+    g = cb.NrLdpc(spec["k"], spec["e"], base_graph=spec["bg"], lifting_size=spec["z"], precision=spec["precision"])
+    llr, _ = g.generate_frames(7, "page_locked", 0, 0, spec["n"], spec["eb"], spec["m"])
+    pinned = torch.empty(llr.shape, dtype=torch.float32 if spec["precision"] == "f32" else torch.float64,
+                         pin_memory=True)
+    pinned.numpy()[:] = llr
+    b1, a1, i1 = g.decode_full(llr)
+    b2, a2, i2 = g.decode_full(pinned.numpy())
+    assert np.array_equal(b1, b2) and np.array_equal(i1, i2)
+    assert np.array_equal(a1.view(np.uint8), a2.view(np.uint8))
+    assert len(set(i1.tolist())) > 2
+
+
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 def test_host_decode_in_chunks_equals_small_calls(cb, precision):
     # cb_decode splits a large host batch into chunks whose copies overlap the decoding of
