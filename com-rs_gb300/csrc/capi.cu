@@ -336,16 +336,26 @@ cb_status copy_back(cb_code* c, int64_t done, int64_t cnt, int wpf, int bpf, uin
   return CB_OK;
 }
 
-// The device address of a host buffer the GPU reads in place (page-locked memory, mapped
-// under unified addressing), or nullptr
+// The address at which `device` reads a host buffer in place (page-locked memory, mapped
+// under unified addressing, and allocated for that device or portable to every device),
+// or nullptr
 template <typename T>
-const T* mapped_host(const T* p) {
+const T* mapped_host(const T* p, int device) {
   cudaPointerAttributes pa;
+  unsigned int flags = 0;
   if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;
   }
-  return pa.type == cudaMemoryTypeHost && pa.devicePointer ? static_cast<const T*>(pa.devicePointer) : nullptr;
+  if (pa.type != cudaMemoryTypeHost || !pa.devicePointer) return nullptr;
+  if (pa.device != device) {
+    if (cudaHostGetFlags(&flags, const_cast<T*>(p)) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    if (!(flags & cudaHostAllocPortable)) return nullptr;
+  }
+  return static_cast<const T*>(pa.devicePointer);
 }
 
 template <typename T>
@@ -355,7 +365,7 @@ cb_status decode_host_impl(cb_code* c, const T* llr, int64_t n, uint8_t* bits, T
   // Page-locked host LLRs: the decoder reads them where they are (over NVLink-C2C on a
   // Grace host), one launch per chunk of frames with no staging copy; only the decisions,
   // a posteriori LLRs and counts come back by copies.
-  if (const T* dev_llr = mapped_host(llr)) {
+  if (const T* dev_llr = mapped_host(llr, c->device)) {
     const int64_t chunk = std::min<int64_t>(n, chunk_frames(c));
     CB_CUDA(c, grow(c->d_bits, c->bits_cap, (size_t)chunk * wpf * 4));
     if (app) CB_CUDA(c, grow(c->d_app, c->app_cap, (size_t)chunk * c->host.k_info * sizeof(T)));
