@@ -23,6 +23,8 @@ CODES = [
     dict(k=8448, e=16896, bg=1, z=384, m=64),       # benchmark config 5
     dict(k=60, e=1000, rv=1, qm=2, m=4),            # repeated bits (E > N_cb)
     dict(k=1000, e=1500, rv=3, qm=6, m=64),         # rv 3, bit interleaver of 6 rows
+    dict(k=1000, e=1502, m=64),                     # 4 padding bits: a last symbol of 2 LLRs
+    dict(k=700, e=1500, m=256),                     # 4 padding bits: a last symbol of 4 LLRs
 ]
 
 
