@@ -157,7 +157,7 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
   __syncthreads();
   // packed info bits for the error counts
   {
-    const int lane = tid & 31, warp = tid >> 5, wpf = (c.k_info + 31) >> 5;
+    const int lane = tid & 31, warp = tid >> 5;
     for (int b0 = warp * 32; b0 < c.k_info; b0 += (NT / 32) * 32) {
       int v = b0 + lane;
       uint32_t word = __ballot_sync(0xffffffffu, v < c.k_info && cw[v]);
@@ -235,7 +235,7 @@ __device__ __forceinline__ void gen_one(const cbd::DevCode& c, const GenFrame<T>
   }
   __syncthreads();
   if (a.cw_out) {  // the full codeword, packed
-    const int lane = tid & 31, warp = tid >> 5, wpc = (c.n_full + 31) >> 5;
+    const int lane = tid & 31, warp = tid >> 5;
     for (int b0 = warp * 32; b0 < c.n_full; b0 += (NT / 32) * 32) {
       int v = b0 + lane;
       uint32_t word = __ballot_sync(0xffffffffu, v < c.n_full && cw[v]);
