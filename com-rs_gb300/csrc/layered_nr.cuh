@@ -557,8 +557,11 @@ __global__ void __launch_bounds__(384, 2) layered_nr_kernel(const __grid_constan
         float a1 = 0.0f, a2 = 0.0f, b1 = 0.0f, b2 = 0.0f;
         uint32_t mt = 0, bt = 0;
         unsigned char* pb = reinterpret_cast<unsigned char*>(post);
+        // (rows 0-3 first in the schedule, in order, 19 entries each; the loop's barrier after
+        // each of them is the schedule's, as each is a level of its own)
         constexpr bool DENSE = decltype(wset)::learned && K::fixed && BG == 1 && Graph<BG>::order[0] == 0 &&
-                               Graph<BG>::order[3] == 3 && Graph<BG>::start[4] == 76;
+                               Graph<BG>::order[1] == 1 && Graph<BG>::order[2] == 2 && Graph<BG>::order[3] == 3 &&
+                               Graph<BG>::start[4] == 76;
         if constexpr (DENSE) {
           // the learned min-sum on base graph 1: rows 0-3 in a rolled loop, then the rest
           const auto w = wset.at(iter - 1);
